@@ -1,0 +1,385 @@
+"""Benchmark: Goofy BC1 + ETC1s encode on GB300, one JSON line on stdout.
+
+Workload (one step): encode one 8192x8192 RGBA8 scene (stride 32768 B,
+seed 1, noise periods x32, 2048 rectangles) with BC1 and with ETC1s -- two
+kernel launches, 2 x 67,108,864 pixels.  Two device copies of the image
+alternate between the codecs, so every launch reads 256 MiB that the
+previous launch did not touch (inputs larger than the 129 MB L2).
+
+* value      -- MPix/s with inputs resident in HBM (device-pointer C ABI),
+                CUDA events around K steps on the launching stream.
+* e2e        -- the same metric through the host C ABI
+                (goofy_gpu_compress_host, the engine under goofy::compress*)
+                from pinned host memory, copies in and out inside the region.
+* roofline   -- dominant kernel: 4.5 algorithmic B/px (4 read + 0.5 written)
+                x pixels per launch / its mean CUDA-event duration, against
+                the measured HBM copy bandwidth.
+* cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
+
+``--impl reference`` times the reference's CPU implementation of the path on
+this host's cores instead (the reference compiled from its own sources where
+they exist, else the oracle port of it), with every host thread.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DXT1/ETC1s MPix/s on 1 GB300 vs HBM roofline, batched vs plain; p50/p99 latency"
+W = H = 8192
+SEED, PERIOD_SCALE, RECTS = 1, 32, 2048
+ALG_BYTES_PER_PX = 4.5
+WORKLOAD = ("plain BC1 + ETC1s encode of one 8192x8192 RGBA8 synthetic scene (stride 32768 B, seed 1, "
+            "value-noise periods x32, 2048 rectangles)")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--soak-s", type=float, default=1.5, help="seconds of the same loop before the timed region "
+                                                             "while clocks are sampled")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic(kernel_key):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.md, a line `traffic <kernel_key> <bytes>`), or None."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(pdir, name)):
+            parts = line.strip().strip("`").split()
+            if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kernel_key:
+                try:
+                    return int(parts[2])
+                except ValueError:
+                    pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_encode_all(lib_fn, img, threads, outs=None):
+    """Both codecs over the whole image; returns seconds."""
+    import numpy as np
+
+    if outs is None:
+        outs = [np.empty((W // 4) * (H // 4) * 8, np.uint8) for _ in range(2)]
+    t0 = time.perf_counter()
+    for codec in (0, 1):
+        rc = lib_fn(codec, outs[codec].ctypes.data, img.ctypes.data, W, H, 4 * W, threads)
+        assert rc > 0, rc
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(img, gpu_outputs, budget_s=12.0):
+    """Oracle port (or the compiled reference where present) on this host's
+    cores: all threads, best of a few full-image passes of both codecs.  The
+    CPU outputs of the last pass double as the check of the GPU outputs."""
+    import numpy as np
+
+    import oracle
+
+    ref = oracle.load_ref()
+    if ref is not None:
+        fn, kind = ref.ref_compress_mt, "reference"
+    else:
+        fn, kind = oracle.load().oracle_compress_mt, "port"
+    cores = os.cpu_count() or 1
+    times = []
+    outs = [np.empty((W // 4) * (H // 4) * 8, np.uint8) for _ in range(2)]
+    t_start = time.perf_counter()
+    while len(times) < 3 or (time.perf_counter() - t_start < budget_s / 2 and len(times) < 20):
+        times.append(cpu_encode_all(fn, img, cores, outs))
+        if time.perf_counter() - t_start > budget_s:
+            break
+    best = min(times)
+    t1 = cpu_encode_all(fn, img, 1)
+    px = 2 * W * H
+    return {"value": round(px / best / 1e6, 1), "unit": "MPix/s", "cores": cores, "kind": kind,
+            "sample": "full 8192x8192 image, BC1 + ETC1s, best of %d passes, block rows striped over %d threads"
+                      % (len(times), cores),
+            "single_thread_mpix_s": round(px / t1 / 1e6, 1),
+            "median_mpix_s": round(px / statistics.median(times) / 1e6, 1),
+            "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from goofy_gb300 import build as lib_build
+    from goofy_gb300 import workloads
+    from oracle import build as oracle_build
+
+    lib_build.build()
+    oracle_build.build()
+    img = workloads.scene(W, H, SEED, PERIOD_SCALE, RECTS, threads=0)
+    import oracle
+
+    ref = oracle.load_ref()
+    fn, kind = (ref.ref_compress_mt, "reference") if ref is not None else (oracle.load().oracle_compress_mt, "port")
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_encode_all(fn, img, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_encode_all(fn, img, cores)
+    dt = time.perf_counter() - t0
+    value = 2 * W * H * args.steps / dt / 1e6
+    line = {"metric": METRIC, "value": round(value, 1), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "pixels_per_step": 2 * W * H,
+                       "implementation": "reference encoder compiled from its sources" if kind == "reference"
+                       else "oracle port of the reference encoder (reference sources absent on this host)"},
+            "cpu_baseline": {"value": round(value, 1), "unit": "MPix/s", "cores": cores, "kind": kind,
+                             "sample": "full 8192x8192 image per step, BC1 + ETC1s, block rows striped over "
+                                       "%d threads" % cores},
+            "e2e": {"value": round(value, 1), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    import goofy_gb300 as g
+    from goofy_gb300 import build as lib_build
+    from goofy_gb300 import workloads
+
+    lib_build.build()
+    assert g.init(local) == g.OK, g.last_error()
+    img = workloads.scene(W, H, SEED, PERIOD_SCALE, RECTS, threads=0)
+    nbytes = img.size
+    dev = torch.device("cuda", local)
+    src = [torch.from_numpy(img.reshape(-1)).to(dev), None]
+    src[1] = src[0].clone()
+    n_out = g.out_size(W, H)
+    dst = [torch.empty(n_out, dtype=torch.uint8, device=dev) for _ in range(2)]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    codecs = (g.CODEC_BC1, g.CODEC_ETC1S)
+
+    def step(events=None):
+        for c in codecs:
+            if events is not None:
+                events[c][0].record(stream)
+            rc = g.compress_device(c, dst[c].data_ptr(), src[c].data_ptr(), W, H, 4 * W, sh)
+            if rc != g.OK:
+                raise RuntimeError("encode failed: %s %s" % (g.status_string(rc), g.last_error()))
+            if events is not None:
+                events[c][1].record(stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    with ClockSampler(local) as clocks:
+        t_soak = time.perf_counter()
+        while time.perf_counter() - t_soak < args.soak_s:
+            for _ in range(20):
+                step()
+            torch.cuda.synchronize()
+        # timed region: K steps, CUDA events on the launching stream
+        per_launch = {c: [] for c in codecs}
+        ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for c in codecs]
+              for _ in range(args.steps)]
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        start.record(stream)
+        for k in range(args.steps):
+            step(ev[k])
+        end.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    total_ms = start.elapsed_time(end)
+    for k in range(args.steps):
+        for c in codecs:
+            per_launch[c].append(ev[k][c][0].elapsed_time(ev[k][c][1]))
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    px_per_step = 2 * W * H
+    value = world * px_per_step * args.steps / (total_ms / 1e3) / 1e6
+
+    # e2e through the host C ABI from pinned memory
+    e2e = None
+    if not args.no_e2e:
+        import ctypes
+
+        p_in = g.host_alloc(nbytes)
+        p_out = g.host_alloc(n_out)
+        try:
+            np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p_in))[:] = img.reshape(-1)
+            for _ in range(2):
+                for c in codecs:
+                    assert g.compress_host(c, p_out, p_in, W, H, 4 * W) == g.OK, g.last_error()
+            e2e_steps = max(3, min(args.steps, 20))
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                for c in codecs:
+                    rc = g.compress_host(c, p_out, p_in, W, H, 4 * W)
+                    if rc != g.OK:
+                        raise RuntimeError(g.last_error())
+            dt = time.perf_counter() - t0
+            if world > 1:
+                t = torch.tensor([dt], dtype=torch.float64)
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                dt = float(t.item())
+            e2e = {"value": round(world * px_per_step * e2e_steps / dt / 1e6, 1), "unit": "MPix/s",
+                   "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * n_out, "steps": e2e_steps,
+                   "api": "goofy_gpu_compress_host (pinned host in/out; the engine of goofy::compressDXT1/ETC1)"}
+        finally:
+            g.host_free(p_in)
+            g.host_free(p_out)
+
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return 0
+
+    peak, peak_kind = read_peaks()
+    names = {g.CODEC_BC1: "bc1", g.CODEC_ETC1S: "etc1s"}
+    per_codec = {}
+    for c in codecs:
+        ms = statistics.mean(per_launch[c])
+        per_codec[names[c]] = {"mean_launch_us": round(1e3 * ms, 2),
+                               "median_launch_us": round(1e3 * statistics.median(per_launch[c]), 2),
+                               "mpix_s": round(W * H / (ms / 1e3) / 1e6, 1),
+                               "hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
+    dom = max(codecs, key=lambda c: statistics.mean(per_launch[c]))
+    dom_ms = statistics.mean(per_launch[dom])
+    achieved = ALG_BYTES_PER_PX * W * H / (dom_ms / 1e3) / 1e9
+    traffic = read_traffic("encode_image_" + names[dom] + "_8192")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "encode_image_kernel<" +
+                names[dom] + ">", "algorithmic_bytes_per_launch": int(ALG_BYTES_PER_PX * W * H),
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s"}
+    cpu = None
+    if not args.no_cpu:
+        from oracle import build as oracle_build
+
+        oracle_build.build()
+        cpu = cpu_baseline(img, [dst[c].cpu().numpy() for c in codecs])
+    tiles = {names[c]: list(g.get_tile(c)) for c in codecs}
+    line = {"metric": METRIC, "value": round(value, 1), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
+                       "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
+                       "tiles": tiles},
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
+            "gpu_launches": 2 * args.steps}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

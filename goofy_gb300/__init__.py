@@ -1,0 +1,188 @@
+"""goofy_gb300 -- GB300-native (sm_103a) Goofy BC1 / ETC1s block encoder.
+
+Python mirror of the reference's public interface (GoofyTC/goofy_tc.h:10-13)
+over the C ABI of ``libgoofy_gb300.so`` (include/goofy_gpu.h):
+
+* ``compressDXT1(result, input, width, height, stride)`` /
+  ``compressETC1(...)`` -- same names, argument meaning and return codes as
+  ``goofy::compressDXT1/compressETC1`` (0, -1 for width % 16, -2 for
+  height % 4); buffers are host memory (numpy arrays, bytearrays or raw
+  addresses).  They run on the GPU; there is no CPU fallback: if the library
+  is not built, importing the functions raises.
+* ``compress_device(codec, dst, src, width, height, stride, stream)`` --
+  device pointers, asynchronous on a CUDA stream (width % 4 is enough).
+* ``compress_host(codec, dst, src, width, height, stride)`` -- host memory,
+  width % 4 is enough.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgoofy_gb300.so")
+SYNTH_PATH = os.path.join(HERE, "_build", "libgoofy_synth.so")
+
+OK = 0
+ERR_WIDTH = -1
+ERR_HEIGHT = -2
+ERR_INVALID = -3
+ERR_ALIGNMENT = -4
+ERR_CUDA = -5
+ERR_NOMEM = -6
+ERR_TIMEOUT = -7
+ERR_BUSY = -8
+ERR_NO_DEVICE = -9
+ERR_TOO_LARGE = -10
+
+CODEC_BC1 = 0
+CODEC_ETC1S = 1
+CODECS = {"bc1": CODEC_BC1, "dxt1": CODEC_BC1, "etc1s": CODEC_ETC1S, "etc1": CODEC_ETC1S}
+
+_lib = None
+_synth = None
+
+_VP = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+
+
+class Tile(ctypes.Structure):
+    _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32)]
+
+
+def _declare(lib):
+    sigs = {
+        "goofy_gpu_init": (ctypes.c_int, [ctypes.c_int]),
+        "goofy_gpu_shutdown": (None, []),
+        "goofy_gpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+        "goofy_gpu_last_error": (ctypes.c_char_p, []),
+        "goofy_gpu_compress_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP]),
+        "goofy_gpu_compress_bc1_device": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32, _VP]),
+        "goofy_gpu_compress_etc1s_device": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32, _VP]),
+        "goofy_gpu_compress_host": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32]),
+        "goofy_gpu_compress_bc1_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
+        "goofy_gpu_compress_etc1s_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
+        "goofy_gpu_host_alloc": (_VP, [ctypes.c_size_t]),
+        "goofy_gpu_host_free": (None, [_VP]),
+        "goofy_gpu_get_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
+        "goofy_gpu_set_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    # C++ drop-in symbols (Itanium mangling of goofy::compressDXT1/ETC1)
+    for mangled in ("_ZN5goofy12compressDXT1EPhPKhjjj", "_ZN5goofy12compressETC1EPhPKhjjj"):
+        fn = getattr(lib, mangled)
+        fn.restype = ctypes.c_int
+        fn.argtypes = [_VP, _VP, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
+    return lib
+
+
+def lib():
+    """The loaded C-ABI library.  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgoofy_gb300.so is not built (run goofy_gb300.build.build()); "
+                               "there is no CPU fallback")
+        _lib = _declare(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            raise RuntimeError("libgoofy_synth.so is not built (run goofy_gb300.build.build())")
+        s = ctypes.CDLL(SYNTH_PATH)
+        s.goofy_synth_scene.restype = ctypes.c_int
+        s.goofy_synth_scene.argtypes = [_VP, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint64,
+                                        ctypes.c_uint, ctypes.c_uint, ctypes.c_int]
+        s.goofy_synth_stress.restype = ctypes.c_int
+        s.goofy_synth_stress.argtypes = [_VP, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint64]
+        s.goofy_synth_downsample.restype = ctypes.c_int
+        s.goofy_synth_downsample.argtypes = [_VP, ctypes.c_uint, _VP, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
+        s.goofy_synth_texture_spec.restype = None
+        s.goofy_synth_texture_spec.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint),
+                                               ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int),
+                                               ctypes.POINTER(ctypes.c_int)]
+        s.goofy_synth_pcg32.restype = ctypes.c_uint32
+        s.goofy_synth_pcg32.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32]
+        _synth = s
+    return _synth
+
+
+def _addr(buf):
+    """Address of a host buffer: numpy array, bytearray, ctypes object or int."""
+    if buf is None:
+        return None
+    if isinstance(buf, int):
+        return buf
+    if hasattr(buf, "ctypes"):  # numpy
+        return buf.ctypes.data
+    if isinstance(buf, bytearray):
+        return ctypes.addressof((ctypes.c_char * len(buf)).from_buffer(buf))
+    if hasattr(buf, "data_ptr"):  # torch tensor
+        return buf.data_ptr()
+    return ctypes.addressof(buf)
+
+
+def status_string(code):
+    return lib().goofy_gpu_status_string(code).decode()
+
+
+def last_error():
+    return lib().goofy_gpu_last_error().decode()
+
+
+# ---- reference-named entry points (goofy_tc.h:10-13) ----
+def compressDXT1(result, input, width, height, stride):
+    """goofy::compressDXT1 on the GPU: host buffers, returns 0 / -1 / -2 (or a GOOFY_ERR_*)."""
+    return lib()._ZN5goofy12compressDXT1EPhPKhjjj(_addr(result), _addr(input), width, height, stride)
+
+
+def compressETC1(result, input, width, height, stride):
+    """goofy::compressETC1 on the GPU: host buffers, returns 0 / -1 / -2 (or a GOOFY_ERR_*)."""
+    return lib()._ZN5goofy12compressETC1EPhPKhjjj(_addr(result), _addr(input), width, height, stride)
+
+
+def compress_host(codec, dst, src, width, height, stride):
+    return lib().goofy_gpu_compress_host(codec, _addr(dst), _addr(src), width, height, stride)
+
+
+def compress_device(codec, dst, src, width, height, stride, stream=None):
+    """Device pointers (ints or torch tensors); `stream` is a cudaStream_t handle (int) or None."""
+    return lib().goofy_gpu_compress_device(codec, _addr(dst), _addr(src), width, height, stride, stream)
+
+
+def init(device=0):
+    return lib().goofy_gpu_init(device)
+
+
+def shutdown():
+    lib().goofy_gpu_shutdown()
+
+
+def host_alloc(nbytes):
+    return lib().goofy_gpu_host_alloc(nbytes)
+
+
+def host_free(ptr):
+    lib().goofy_gpu_host_free(ptr)
+
+
+def get_tile(codec):
+    t = Tile()
+    rc = lib().goofy_gpu_get_tile(codec, ctypes.byref(t))
+    if rc != OK:
+        raise ValueError(status_string(rc))
+    return (t.threads_per_cta, t.blocks_per_thread)
+
+
+def set_tile(codec, threads_per_cta, blocks_per_thread):
+    t = Tile(threads_per_cta, blocks_per_thread)
+    return lib().goofy_gpu_set_tile(codec, ctypes.byref(t))
+
+
+def out_size(width, height):
+    """Bytes of encoded output: (width/4)*(height/4) blocks of 8 bytes."""
+    return (width // 4) * (height // 4) * 8

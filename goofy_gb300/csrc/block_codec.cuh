@@ -1,0 +1,224 @@
+// block_codec.cuh -- per-4x4-block Goofy encoder for sm_103a, integer SIMT.
+//
+// One thread encodes one block from its 16 RGBA8 pixel words (row-major,
+// byte 0 = R).  The arithmetic is the reference heuristic
+// (GoofyTC/goofy_tc.h:1066-1494, goofySimdEncode) restated for 32-bit
+// registers instead of 16-byte SSE2 vectors; results are bit-identical.
+//
+// Identities the formulation relies on (all exact on 0..255 inputs):
+//  * luma  Y(c) = avg(avg(R, B), G)  with avg(a,b) = (a+b+1)>>1
+//          (goofy_tc.h:1159-1166) equals ceil((R + 2G + B) / 4).  Writing
+//          S = R + 2G + B (one dp4a against bytes 1,2,1,0):
+//             Y >= c   <=>   S >= 4c - 3      for every integer c,
+//          so every per-pixel brightness test is one add of a per-block
+//          constant followed by a look at one bit.
+//  * gez = (Y >= mid); lqt = |Y - mid| < qt <=> (Y >= mid-qt+1) && !(Y >= mid+qt)
+//          (qt <= 96 < 127, so the clamp to 127 at goofy_tc.h:1207-1208 and
+//          the signed compare at :1224 never change the outcome).
+//  * to5(x) = avg(avg(avg(subsat(x,8),0),0),0)  (goofy_tc.h:1309)
+//           = (max(x,1) - 1) >> 3.
+//  * the ETC1 mean tree of rounding averages (goofy_tc.h:1402-1414) is kept
+//    exact in 16-bit lanes by carrying each level scaled by 2^k:
+//           2^k * avg(x, y) = (2^(k-1) x + 2^(k-1) y + 2^(k-1)) & ~(2^k - 1).
+#pragma once
+#include <cstdint>
+
+#if defined(GOOFY_HOST_EMULATION)
+// Test-only: lets tests/host_emu compile this header for the CPU to check the
+// block arithmetic against the oracle without a GPU.  Never part of the
+// shipped library, which is built for sm_103a only.
+#include "host_emulation.h"
+#else
+#define GOOFY_FN __device__ __forceinline__
+#endif
+
+namespace goofy_gpu {
+
+enum Codec : int { kBC1 = 0, kETC1S = 1 };
+
+#if !defined(GOOFY_HOST_EMULATION)
+GOOFY_FN uint32_t perm(uint32_t a, uint32_t b, uint32_t sel) { return __byte_perm(a, b, sel); }
+
+GOOFY_FN uint32_t vmin2(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+GOOFY_FN uint32_t vmax2(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+#endif
+
+// S = R + 2G + B + acc
+GOOFY_FN uint32_t luma_sum(uint32_t px, uint32_t acc) { return __dp4a(px, 0x00010201u, acc); }
+
+// Y = avg(avg(R,B),G) of an RGB word
+GOOFY_FN uint32_t luma(uint32_t px) { return luma_sum(px, 3u) >> 2; }
+
+// to5 on both 16-bit lanes
+GOOFY_FN uint32_t to5x2(uint32_t lanes) { return ((vmax2(lanes, 0x00010001u) - 0x00010001u) >> 3) & 0x001f001fu; }
+
+template <int N>
+GOOFY_FN uint32_t tree_min(const uint32_t* v)
+{
+    if constexpr (N == 1) return v[0];
+    else return vmin2(tree_min<N / 2>(v), tree_min<N / 2>(v + N / 2));
+}
+
+template <int N>
+GOOFY_FN uint32_t tree_max(const uint32_t* v)
+{
+    if constexpr (N == 1) return v[0];
+    else return vmax2(tree_max<N / 2>(v), tree_max<N / 2>(v + N / 2));
+}
+
+// Run starts of etc1BrighnessRangeTocontrolByte (goofy_tc.h:1040-1057); all
+// are even, so a 128-entry table indexed by range>>1 reproduces it.
+GOOFY_FN uint32_t etc_control_byte(uint32_t range)
+{
+    const uint32_t t = (range >= 22) + (range >= 44) + (range >= 74) + (range >= 106) + (range >= 152) +
+                       (range >= 182) + (range >= 254);
+    return t * 0x24u + 3u;  // (t<<5)|(t<<2)|diff|flip
+}
+
+struct BlockRange {
+    uint32_t range, mid, qt;
+};
+
+// Brightness statistics of the block from its channel min / max words
+// (bytes R,G,B,x), goofy_tc.h:1151-1190.
+GOOFY_FN BlockRange block_range(uint32_t mn_rgb, uint32_t mx_rgb)
+{
+    const uint32_t ymin = luma(mn_rgb), ymax = luma(mx_rgb);
+    BlockRange r;
+    r.range = max(ymax - ymin, 8u);
+    r.mid = (ymin + ymax + 1u) >> 1;
+    const uint32_t quarter = (((r.range + 1u) >> 1) + 1u) >> 1;
+    r.qt = quarter + ((quarter + 1u) >> 1);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// BC1: returns {c0 | c1 << 16, indices}; pixel i (row-major) at bits 2i..2i+1.
+// goofy_tc.h:1276-1357.
+// ---------------------------------------------------------------------------
+GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
+{
+    uint32_t rb[16], gg[8];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) rb[i] = w[i] & 0x00ff00ffu;           // lanes R, B
+#pragma unroll
+    for (int k = 0; k < 8; ++k) gg[k] = perm(w[k], w[k + 8], 0x5511u);  // lanes 257*G of two pixels
+    const uint32_t mn_rb = tree_min<16>(rb), mx_rb = tree_max<16>(rb);
+    uint32_t mn_g = tree_min<8>(gg), mx_g = tree_max<8>(gg);
+    mn_g = vmin2(mn_g, mn_g >> 16);  // byte 0 = min G
+    mx_g = vmax2(mx_g, mx_g >> 16);
+    const BlockRange br = block_range(perm(mn_rb, mn_g, 0x1240u), perm(mx_rb, mx_g, 0x1240u));
+
+    // thresholds on S of two pixels at once (16-bit lanes): flag bits 14 / 15
+    const uint32_t k_gez = (0x4003u - 4u * br.mid) * 0x10001u;                // bit 14: Y >= mid
+    const uint32_t k_lo = (0x8003u - 4u * (br.mid - br.qt + 1u)) * 0x10001u;  // bit 15: Y >= mid-qt+1
+    const uint32_t k_hi = (0x8003u - 4u * (br.mid + br.qt)) * 0x10001u;       // bit 15: Y >= mid+qt
+    uint32_t idx = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {  // pixels i and i+8 share a register
+        const uint32_t s = perm(luma_sum(w[i], 0u), luma_sum(w[i + 8], 0u), 0x5410u);
+        const uint32_t f_gez = s + k_gez, f_lo = s + k_lo, f_hi = s + k_hi;
+        // bit 14: not gez, bit 15: lqt (and 30 / 31 for pixel i+8)
+        const uint32_t z = (f_lo & ~f_hi & 0x80008000u) | (~f_gez & 0x40004000u);
+        idx += i < 7 ? __umulhi(z, 1u << (18 + 2 * i)) : z;  // z >> (14 - 2i)
+    }
+
+    // endpoints: lanes {max, min} for each channel, c0 in the low half
+    const uint32_t r5 = to5x2(perm(mx_rb, mn_rb, 0x5410u));
+    const uint32_t b5 = to5x2(perm(mx_rb, mn_rb, 0x7632u));
+    const uint32_t g5 = to5x2(perm(mx_g, mn_g, 0x0400u) & 0x00ff00ffu);
+    const uint32_t ends = (r5 << 11) | (g5 << 6) | b5 | 0x20u;
+    return make_uint2(ends, idx);
+}
+
+// ---------------------------------------------------------------------------
+// ETC1s: returns {word0, word1} as the reference stores them (little-endian
+// u32s of the big-endian ETC1 block).  goofy_tc.h:1358-1493.
+// `ctrl_lut` holds etc_control_byte(2*i) for i < 128.
+// ---------------------------------------------------------------------------
+GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
+{
+    uint32_t rb[16], gp[8];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) rb[i] = w[i] & 0x00ff00ffu;
+#pragma unroll
+    for (int y = 0; y < 4; ++y)
+#pragma unroll
+        for (int x = 0; x < 2; ++x)  // lanes G(y, x), G(y, x+2)
+            gp[2 * y + x] = perm(w[4 * y + x], w[4 * y + x + 2], 0x0501u) & 0x00ff00ffu;
+    const uint32_t mn_rb = tree_min<16>(rb), mx_rb = tree_max<16>(rb);
+    uint32_t mn_g = tree_min<8>(gp), mx_g = tree_max<8>(gp);
+    mn_g = vmin2(mn_g, mn_g >> 16);
+    mx_g = vmax2(mx_g, mx_g >> 16);
+    const BlockRange br = block_range(perm(mn_rb, mn_g, 0x1240u), perm(mx_rb, mx_g, 0x1240u));
+
+    // block mean, rounding-average tree kept exact at scale 2^level
+    uint32_t col_rb[4];
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+        const uint32_t a = (rb[x] + rb[4 + x] + 0x00010001u) & 0xfffefffeu;
+        const uint32_t b = (rb[8 + x] + rb[12 + x] + 0x00010001u) & 0xfffefffeu;
+        col_rb[x] = (a + b + 0x00020002u) & 0xfffcfffcu;
+    }
+    const uint32_t u_rb = (col_rb[0] + col_rb[1] + 0x00040004u) & 0xfff8fff8u;
+    const uint32_t v_rb = (col_rb[2] + col_rb[3] + 0x00040004u) & 0xfff8fff8u;
+    const uint32_t m_rb = ((u_rb + v_rb + 0x00080008u) & 0xfff0fff0u) >> 4;  // lanes mean R, mean B
+    uint32_t col_g[2];
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+        const uint32_t a = (gp[x] + gp[2 + x] + 0x00010001u) & 0xfffefffeu;
+        const uint32_t b = (gp[4 + x] + gp[6 + x] + 0x00010001u) & 0xfffefffeu;
+        col_g[x] = (a + b + 0x00020002u) & 0xfffcfffcu;  // lanes 4*col(x), 4*col(x+2)
+    }
+    const uint32_t uv_g = (col_g[0] + col_g[1] + 0x00040004u) & 0xfff8fff8u;
+    const uint32_t m_g = ((uv_g + (uv_g >> 16) + 8u) & 0xfff0u) >> 4;
+
+    // move the mean's brightness onto mid, goofy_tc.h:1416-1449
+    const uint32_t ya = luma(perm(m_rb, m_g, 0x1240u));
+    const bool up = ya <= br.mid;
+    const uint32_t corr = min(up ? br.mid - ya : ya - br.mid, 0x7fu);
+    const uint32_t corr2 = corr * 0x00010001u;
+    const uint32_t base_rb = up ? vmin2(m_rb + corr2, 0x00ff00ffu) : vmax2(m_rb, corr2) - corr2;
+    const uint32_t base_g = up ? min(m_g + corr, 0xffu) : max(m_g, corr) - corr;
+    const uint32_t rb5 = to5x2(base_rb);
+    const uint32_t g5 = to5x2(base_g);
+    const uint32_t word0 = (uint32_t)ctrl_lut[br.range >> 1] << 24 | rb5 << 3 | g5 << 11;
+
+    // indices: bit j = not gez, bit 16+j = not lqt of the pixel with
+    // j = 4*(x^2) + y (transposeAs4x4x4 order, goofy_tc.h:1366-1395)
+    const uint32_t k_q = (0x8003u - 4u * br.mid) | (0x8003u - 4u * (br.mid - br.qt + 1u)) << 16;
+    const uint32_t k_h = (0x8003u - 4u * (br.mid + br.qt)) << 16;
+    uint32_t word1 = 0;
+#pragma unroll
+    for (int y = 0; y < 4; ++y)
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+            const int j = 4 * (x ^ 2) + y;
+            const uint32_t s = luma_sum(w[4 * y + x], 0u);
+            const uint32_t q = s * 0x00010001u + k_q;  // bit 15: Y >= mid, bit 31: Y >= mid-qt+1
+            const uint32_t h = s * 0x00010000u + k_h;  // bit 31: Y >= mid+qt, bits 0..15 zero
+            const uint32_t z = (~q | h) & 0x80008000u;
+            word1 += j < 15 ? __umulhi(z, 1u << (17 + j)) : z;  // z >> (15 - j)
+        }
+    return make_uint2(word0, word1);
+}
+
+template <int CODEC>
+GOOFY_FN uint2 encode_block(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
+{
+    if constexpr (CODEC == kBC1) return encode_bc1(w);
+    else return encode_etc1s(w, ctrl_lut);
+}
+
+}  // namespace goofy_gpu

@@ -1,0 +1,382 @@
+// capi.cpp -- C ABI, host-pointer pipeline and the C++ drop-in entry points.
+//
+// Reference interface replaced: goofy::compressDXT1 / goofy::compressETC1
+// (GoofyTC/goofy_tc.h:10-13, :1497-1557), a synchronous CPU function over
+// caller-owned host buffers.  Here the same call streams the image through
+// the GPU: the rows are split into bands, and for each band
+//   host -> device copy, encode kernel, device -> host copy
+// are queued on one of two streams, so the copy-in of band b+1 overlaps the
+// encode and copy-out of band b.  Pinned caller buffers are copied by DMA
+// directly; pageable ones go through library-owned pinned staging.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/goofy_gpu.h"
+#include "../../include/goofy_tc_gpu.h"
+#include "kernels.h"
+
+#define GOOFY_EXPORT __attribute__((visibility("default")))
+
+namespace {
+
+using goofy_gpu::SrcAccess;
+using goofy_gpu::Tile;
+
+thread_local char g_last_error[256] = "";
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GOOFY_ERR_NOMEM
+           : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? GOOFY_ERR_NO_DEVICE
+                                                                           : GOOFY_ERR_CUDA;
+}
+
+#define CUDA_TRY(call)                                        \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+Tile g_tile[2] = {{256, 2}, {256, 2}};
+std::mutex g_tile_mu;
+
+Tile tile_for(int codec)
+{
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    return g_tile[codec & 1];
+}
+
+struct Buffer {
+    uint8_t* p = nullptr;
+    size_t cap = 0;
+};
+
+// Per-process state of the host-pointer path.
+struct HostPath {
+    std::mutex mu;
+    bool ready = false;
+    int device = 0;
+    cudaStream_t stream[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    Buffer d_src[2], d_dst[2], h_src[2], h_dst[2];
+
+    int ensure_device(Buffer& b, size_t bytes)
+    {
+        if (b.cap >= bytes) return GOOFY_OK;
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        CUDA_TRY(cudaMalloc(&b.p, bytes));
+        b.cap = bytes;
+        return GOOFY_OK;
+    }
+
+    int ensure_pinned(Buffer& b, size_t bytes)
+    {
+        if (b.cap >= bytes) return GOOFY_OK;
+        if (b.p) cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        CUDA_TRY(cudaHostAlloc(&b.p, bytes, cudaHostAllocDefault));
+        b.cap = bytes;
+        return GOOFY_OK;
+    }
+
+    int init_locked(int dev)
+    {
+        if (ready && dev == device) return GOOFY_OK;
+        release_locked();
+        int n = 0;
+        CUDA_TRY(cudaGetDeviceCount(&n));
+        if (dev < 0 || dev >= n) return GOOFY_ERR_NO_DEVICE;
+        DeviceGuard g(dev);
+        CUDA_TRY(g.err);
+        device = dev;
+        for (int i = 0; i < 2; ++i) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&stream[i], cudaStreamNonBlocking));
+            CUDA_TRY(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
+        }
+        ready = true;
+        return GOOFY_OK;
+    }
+
+    void release_locked()
+    {
+        if (!ready) return;
+        DeviceGuard g(device);
+        for (int i = 0; i < 2; ++i) {
+            if (stream[i]) cudaStreamSynchronize(stream[i]);
+            if (d_src[i].p) cudaFree(d_src[i].p);
+            if (d_dst[i].p) cudaFree(d_dst[i].p);
+            if (h_src[i].p) cudaFreeHost(h_src[i].p);
+            if (h_dst[i].p) cudaFreeHost(h_dst[i].p);
+            d_src[i] = d_dst[i] = h_src[i] = h_dst[i] = Buffer{};
+            if (done[i]) cudaEventDestroy(done[i]);
+            if (stream[i]) cudaStreamDestroy(stream[i]);
+            done[i] = nullptr;
+            stream[i] = nullptr;
+        }
+        ready = false;
+    }
+};
+
+HostPath& host_path()
+{
+    static HostPath* hp = new HostPath();  // never destroyed: no CUDA calls at static teardown
+    return *hp;
+}
+
+bool is_pinned(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+int check_args(int codec, const void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride)
+{
+    if (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S) return GOOFY_ERR_INVALID;
+    if (width % 4 != 0) return GOOFY_ERR_WIDTH;
+    if (height % 4 != 0) return GOOFY_ERR_HEIGHT;
+    if (width == 0 || height == 0) return GOOFY_OK;
+    if (!dst || !src) return GOOFY_ERR_INVALID;
+    if ((uint64_t)stride < 4ull * width) return GOOFY_ERR_INVALID;
+    return 1;  // proceed
+}
+
+constexpr size_t kBandBytes = 16u << 20;  // source bytes per band of the host path
+
+int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height, uint32_t stride)
+{
+    int rc = check_args(codec, dst, src, width, height, stride);
+    if (rc <= 0) return rc;
+    HostPath& hp = host_path();
+    std::lock_guard<std::mutex> lk(hp.mu);
+    if (!hp.ready) {
+        rc = hp.init_locked(hp.device);
+        if (rc != GOOFY_OK) return rc;
+    }
+    DeviceGuard g(hp.device);
+    CUDA_TRY(g.err);
+
+    const uint32_t bw = width / 4, bh = height / 4;
+    const size_t row_bytes = 4ull * width;
+    const size_t dpitch = (row_bytes + 15) & ~size_t(15);  // device / staging pitch: 16-byte rows
+    const uint32_t band_bh = (uint32_t)std::max<size_t>(1, std::min<size_t>(bh, kBandBytes / (4 * dpitch)));
+    const uint32_t nbands = (bh + band_bh - 1) / band_bh;
+    const bool src_pinned = is_pinned(src), dst_pinned = is_pinned(dst);
+    const size_t band_in = (size_t)band_bh * 4 * dpitch, band_out = (size_t)band_bh * bw * 8;
+    const int slots = nbands > 1 ? 2 : 1;
+    for (int s = 0; s < slots; ++s) {
+        if ((rc = hp.ensure_device(hp.d_src[s], band_in)) != GOOFY_OK) return rc;
+        if ((rc = hp.ensure_device(hp.d_dst[s], band_out)) != GOOFY_OK) return rc;
+        if (!src_pinned && (rc = hp.ensure_pinned(hp.h_src[s], band_in)) != GOOFY_OK) return rc;
+        if (!dst_pinned && (rc = hp.ensure_pinned(hp.h_dst[s], band_out)) != GOOFY_OK) return rc;
+    }
+    const Tile tile = tile_for(codec);
+
+    // band b: rows [b*band_bh, ...); slot b % slots.  A slot is reused only
+    // after its previous band finished (and, for pageable dst, was copied out).
+    auto finish_band = [&](uint32_t b) -> int {
+        const int s = (int)(b % slots);
+        CUDA_TRY(cudaEventSynchronize(hp.done[s]));
+        if (!dst_pinned) {
+            const uint32_t rows = std::min(band_bh, bh - b * band_bh);
+            std::memcpy(dst + (size_t)b * band_bh * bw * 8, hp.h_dst[s].p, (size_t)rows * bw * 8);
+        }
+        return GOOFY_OK;
+    };
+    for (uint32_t b = 0; b < nbands; ++b) {
+        const int s = (int)(b % slots);
+        if (b >= (uint32_t)slots && (rc = finish_band(b - slots)) != GOOFY_OK) return rc;
+        const uint32_t rows = std::min(band_bh, bh - b * band_bh);
+        const uint8_t* sb = src + (size_t)b * band_bh * 4 * stride;
+        cudaStream_t st = hp.stream[s];
+        if (src_pinned) {
+            CUDA_TRY(cudaMemcpy2DAsync(hp.d_src[s].p, dpitch, sb, stride, row_bytes, (size_t)rows * 4,
+                                       cudaMemcpyHostToDevice, st));
+        } else {
+            uint8_t* stage = hp.h_src[s].p;
+            for (size_t y = 0; y < (size_t)rows * 4; ++y) std::memcpy(stage + y * dpitch, sb + y * stride, row_bytes);
+            CUDA_TRY(cudaMemcpyAsync(hp.d_src[s].p, stage, (size_t)rows * 4 * dpitch, cudaMemcpyHostToDevice, st));
+        }
+        CUDA_TRY(goofy_gpu::launch_image(codec, hp.d_src[s].p, dpitch, hp.d_dst[s].p, width, rows * 4, tile,
+                                         SrcAccess::kVec16, st));
+        uint8_t* out = dst_pinned ? dst + (size_t)b * band_bh * bw * 8 : hp.h_dst[s].p;
+        CUDA_TRY(cudaMemcpyAsync(out, hp.d_dst[s].p, (size_t)rows * bw * 8, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaEventRecord(hp.done[s], st));
+    }
+    for (uint32_t b = nbands > (uint32_t)slots ? nbands - slots : 0; b < nbands; ++b)
+        if ((rc = finish_band(b)) != GOOFY_OK) return rc;
+    return GOOFY_OK;
+}
+
+int compress_device_impl(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
+                         void* stream)
+{
+    int rc = check_args(codec, dst, src, width, height, stride);
+    if (rc <= 0) return rc;
+    if (reinterpret_cast<uintptr_t>(dst) % 8 != 0) return GOOFY_ERR_ALIGNMENT;
+    const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+    SrcAccess access;
+    if (s % 16 == 0 && stride % 16 == 0) access = SrcAccess::kVec16;
+    else if (s % 4 == 0 && stride % 4 == 0) access = SrcAccess::kWord4;
+    else return GOOFY_ERR_ALIGNMENT;
+    CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
+                                     width, height, tile_for(codec), access, static_cast<cudaStream_t>(stream)));
+    return GOOFY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GOOFY_EXPORT int goofy_gpu_init(int device)
+{
+    HostPath& hp = host_path();
+    std::lock_guard<std::mutex> lk(hp.mu);
+    return hp.init_locked(device);
+}
+
+GOOFY_EXPORT void goofy_gpu_shutdown(void)
+{
+    HostPath& hp = host_path();
+    std::lock_guard<std::mutex> lk(hp.mu);
+    hp.release_locked();
+}
+
+GOOFY_EXPORT const char* goofy_gpu_status_string(int status)
+{
+    switch (status) {
+    case GOOFY_OK: return "ok";
+    case GOOFY_ERR_WIDTH: return "width is not a multiple of the block width";
+    case GOOFY_ERR_HEIGHT: return "height is not a multiple of 4";
+    case GOOFY_ERR_INVALID: return "invalid argument";
+    case GOOFY_ERR_ALIGNMENT: return "misaligned pointer or stride";
+    case GOOFY_ERR_CUDA: return "CUDA error";
+    case GOOFY_ERR_NOMEM: return "out of memory";
+    case GOOFY_ERR_TIMEOUT: return "timed out";
+    case GOOFY_ERR_BUSY: return "busy";
+    case GOOFY_ERR_NO_DEVICE: return "no CUDA device";
+    case GOOFY_ERR_TOO_LARGE: return "request exceeds capacity";
+    default: return "unknown status";
+    }
+}
+
+GOOFY_EXPORT const char* goofy_gpu_last_error(void) { return g_last_error; }
+
+GOOFY_EXPORT int goofy_gpu_compress_device(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
+                                           uint32_t stride, void* stream)
+{
+    return compress_device_impl(codec, dst, src, width, height, stride, stream);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_bc1_device(void* dst, const void* src, uint32_t width, uint32_t height,
+                                               uint32_t stride, void* stream)
+{
+    return compress_device_impl(GOOFY_CODEC_BC1, dst, src, width, height, stride, stream);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_etc1s_device(void* dst, const void* src, uint32_t width, uint32_t height,
+                                                 uint32_t stride, void* stream)
+{
+    return compress_device_impl(GOOFY_CODEC_ETC1S, dst, src, width, height, stride, stream);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_t width,
+                                         uint32_t height, uint32_t stride)
+{
+    return compress_host_impl(codec, dst, src, width, height, stride);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_bc1_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
+                                             uint32_t stride)
+{
+    return compress_host_impl(GOOFY_CODEC_BC1, dst, src, width, height, stride);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
+                                               uint32_t stride)
+{
+    return compress_host_impl(GOOFY_CODEC_ETC1S, dst, src, width, height, stride);
+}
+
+GOOFY_EXPORT void* goofy_gpu_host_alloc(size_t bytes)
+{
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+GOOFY_EXPORT void goofy_gpu_host_free(void* p)
+{
+    if (p) cudaFreeHost(p);
+}
+
+GOOFY_EXPORT int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile)
+{
+    if (!tile || (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S)) return GOOFY_ERR_INVALID;
+    const Tile t = tile_for(codec);
+    tile->threads_per_cta = t.threads;
+    tile->blocks_per_thread = t.bpt;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile)
+{
+    if (!tile || (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S)) return GOOFY_ERR_INVALID;
+    const Tile t{tile->threads_per_cta, tile->blocks_per_thread};
+    if (!goofy_gpu::tile_valid(t)) return GOOFY_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    g_tile[codec] = t;
+    return GOOFY_OK;
+}
+
+}  // extern "C"
+
+// ---- C++ drop-in: goofy::compressDXT1 / compressETC1 (goofy_tc.h:10-13) ----
+namespace goofy {
+
+GOOFY_EXPORT int compressDXT1(unsigned char* result, const unsigned char* input, unsigned int width,
+                              unsigned int height, unsigned int stride)
+{
+    if (width % 16 != 0) return -1;  // goofy_tc.h:1500-1503
+    if (height % 4 != 0) return -2;  // goofy_tc.h:1505-1508
+    return compress_host_impl(GOOFY_CODEC_BC1, result, input, width, height, stride);
+}
+
+GOOFY_EXPORT int compressETC1(unsigned char* result, const unsigned char* input, unsigned int width,
+                              unsigned int height, unsigned int stride)
+{
+    if (width % 16 != 0) return -1;  // goofy_tc.h:1531-1534
+    if (height % 4 != 0) return -2;  // goofy_tc.h:1536-1539
+    return compress_host_impl(GOOFY_CODEC_ETC1S, result, input, width, height, stride);
+}
+
+}  // namespace goofy

@@ -1,0 +1,140 @@
+// encode_kernels.cu -- image encoder kernels for sm_103a.
+//
+// Replaces the reference's image driver loops (goofy::compressDXT1 /
+// compressETC1, GoofyTC/goofy_tc.h:1497-1557: block rows x 16-pixel strips,
+// 4 blocks per goofySimdEncode call) with a grid over 4x4 blocks.
+//
+// Mapping: one warp owns a segment of 32*BPT consecutive blocks of one block
+// row; lane l encodes blocks l, l+32, ..., l+32*(BPT-1) of the segment.  For
+// each of the 4 pixel rows a warp-wide 128-bit load instruction therefore
+// reads 512 contiguous bytes (every 32-byte sector fully used), and each
+// 8-byte block store of the warp writes 256 contiguous bytes.  Source rows are
+// read once (L1 no-allocate) and blocks are written with streaming stores:
+// the kernel moves 4 B/px in and 0.5 B/px out and is meant to sit on the HBM
+// roofline.
+#include <cuda_runtime.h>
+
+#include "block_codec.cuh"
+#include "kernels.h"
+
+namespace goofy_gpu {
+
+__device__ __forceinline__ uint4 ld_once16(const uint8_t* p)
+{
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint32_t ld_once4(const uint8_t* p)
+{
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void st_stream8(uint8_t* p, uint2 v)
+{
+    asm volatile("st.global.cs.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.x), "r"(v.y) : "memory");
+}
+
+template <SrcAccess ACCESS>
+__device__ __forceinline__ void load_block(const uint8_t* p, size_t stride, uint32_t (&w)[16])
+{
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+        const uint8_t* r = p + (size_t)y * stride;
+        if constexpr (ACCESS == SrcAccess::kVec16) {
+            const uint4 v = ld_once16(r);
+            w[4 * y + 0] = v.x;
+            w[4 * y + 1] = v.y;
+            w[4 * y + 2] = v.z;
+            w[4 * y + 3] = v.w;
+        } else {
+#pragma unroll
+            for (int x = 0; x < 4; ++x) w[4 * y + x] = ld_once4(r + 4 * x);
+        }
+    }
+}
+
+__device__ __forceinline__ void fill_ctrl_lut(uint8_t* lut)
+{
+    for (uint32_t i = threadIdx.x; i < 128; i += blockDim.x) lut[i] = (uint8_t)etc_control_byte(2 * i);
+}
+
+template <int CODEC, int BPT, SrcAccess ACCESS>
+__global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __restrict__ src, size_t stride,
+                                                           uint8_t* __restrict__ dst, uint32_t bw, uint32_t bh,
+                                                           uint32_t segs_per_row)
+{
+    __shared__ uint8_t ctrl_lut[128];
+    if constexpr (CODEC == kETC1S) {
+        fill_ctrl_lut(ctrl_lut);
+        __syncthreads();
+    }
+    const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t by = warp / segs_per_row;
+    if (by >= bh) return;
+    const uint32_t bx0 = (warp - by * segs_per_row) * (32u * BPT) + (threadIdx.x & 31u);
+    const uint8_t* row = src + (size_t)by * 4u * stride;
+
+    uint32_t w[BPT][16];
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t bx = bx0 + 32u * j;
+        if (bx < bw) load_block<ACCESS>(row + 16u * (size_t)bx, stride, w[j]);
+    }
+    uint8_t* out = dst + (size_t)by * bw * 8u;
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t bx = bx0 + 32u * j;
+        if (bx < bw) st_stream8(out + 8u * (size_t)bx, encode_block<CODEC>(w[j], ctrl_lut));
+    }
+}
+
+template <int CODEC, int BPT, SrcAccess ACCESS>
+static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+                            uint32_t threads, cudaStream_t stream)
+{
+    const uint32_t segs = (bw + 32u * BPT - 1) / (32u * BPT);
+    const uint64_t warps = (uint64_t)segs * bh;
+    const uint32_t wpc = threads / 32u;
+    const uint64_t ctas = (warps + wpc - 1) / wpc;
+    if (ctas > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    encode_image_kernel<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(src, stride, dst, bw, bh, segs);
+    return cudaGetLastError();
+}
+
+template <int CODEC, SrcAccess ACCESS>
+static cudaError_t launch_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh, Tile tile,
+                              cudaStream_t stream)
+{
+    switch (tile.bpt) {
+    case 1: return launch_t<CODEC, 1, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
+    case 2: return launch_t<CODEC, 2, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
+    case 4: return launch_t<CODEC, 4, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int CODEC>
+static cudaError_t launch_access(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+                                 Tile tile, SrcAccess access, cudaStream_t stream)
+{
+    if (access == SrcAccess::kVec16) return launch_bpt<CODEC, SrcAccess::kVec16>(src, stride, dst, bw, bh, tile, stream);
+    return launch_bpt<CODEC, SrcAccess::kWord4>(src, stride, dst, bw, bh, tile, stream);
+}
+
+cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
+                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream)
+{
+    if (!tile_valid(tile)) return cudaErrorInvalidValue;
+    const uint32_t bw = width / 4, bh = height / 4;
+    if (bw == 0 || bh == 0) return cudaSuccess;
+    if (codec == kBC1) return launch_access<kBC1>(src, stride, dst, bw, bh, tile, access, stream);
+    return launch_access<kETC1S>(src, stride, dst, bw, bh, tile, access, stream);
+}
+
+}  // namespace goofy_gpu

@@ -1,0 +1,32 @@
+// kernels.h -- host-side launchers of the encoder kernels (internal C++ API
+// between the C-ABI layer and the CUDA translation unit).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace goofy_gpu {
+
+struct Tile {
+    uint32_t threads;  // threads per CTA: 128, 256 or 512
+    uint32_t bpt;      // 4x4 blocks per thread: 1, 2 or 4
+};
+
+inline bool tile_valid(const Tile& t)
+{
+    return (t.threads == 128 || t.threads == 256 || t.threads == 512) && (t.bpt == 1 || t.bpt == 2 || t.bpt == 4);
+}
+
+// How the image kernel reads its source rows.
+enum class SrcAccess : int {
+    kVec16 = 0,  // 16-byte aligned base and stride: one 128-bit load per block row
+    kWord4 = 1,  // 4-byte aligned: four 32-bit loads per block row
+};
+
+// Encode a whole image (width, height multiples of 4) into row-major 8-byte
+// blocks at `dst`.  Only enqueues; returns the launch error, if any.
+cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
+                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream);
+
+}  // namespace goofy_gpu

@@ -1,0 +1,106 @@
+/*
+ * goofy_gpu.h -- C ABI of the GB300 (sm_103a) Goofy BC1 / ETC1s block encoder.
+ *
+ * Plain pointers and sizes only; `stream` arguments are cudaStream_t passed as
+ * void* (NULL = the legacy default stream).  Every function returns a status
+ * code (GOOFY_OK or a negative GOOFY_ERR_*).
+ *
+ * Output format and bits are those of the reference goofy::compressDXT1 /
+ * goofy::compressETC1 (GoofyTC/goofy_tc.h:10-13, defined at :1497-1557):
+ * (width/4)*(height/4) blocks of 8 bytes, row-major, no destination pitch.
+ */
+#ifndef GOOFY_GPU_H
+#define GOOFY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GOOFY_OK 0
+#define GOOFY_ERR_WIDTH (-1)     /* same code as the reference (goofy_tc.h:1500-1503) */
+#define GOOFY_ERR_HEIGHT (-2)    /* same code as the reference (goofy_tc.h:1505-1508) */
+#define GOOFY_ERR_INVALID (-3)   /* null pointer, stride < 4*width, bad codec, ... */
+#define GOOFY_ERR_ALIGNMENT (-4) /* device source not 4-byte aligned / dst not 8-byte aligned */
+#define GOOFY_ERR_CUDA (-5)      /* a CUDA runtime call failed; see goofy_gpu_last_error() */
+#define GOOFY_ERR_NOMEM (-6)     /* device or pinned host allocation failed */
+#define GOOFY_ERR_TIMEOUT (-7)   /* a bounded wait expired */
+#define GOOFY_ERR_BUSY (-8)      /* queue / admission budget exhausted */
+#define GOOFY_ERR_NO_DEVICE (-9) /* no usable CUDA device */
+#define GOOFY_ERR_TOO_LARGE (-10) /* request exceeds a fixed capacity */
+
+#define GOOFY_CODEC_BC1 0   /* DXT1 / BC1, goofySimdEncode<GOOFY_DXT1> */
+#define GOOFY_CODEC_ETC1S 1 /* ETC1s, goofySimdEncode<GOOFY_ETC1> */
+
+/* ---- library -------------------------------------------------------------- */
+
+/* Select the device the host-pointer entry points use (default: device 0) and
+ * create its streams.  Optional: the first host call initialises lazily.
+ * No reference counterpart (the reference is a pure CPU function). */
+int goofy_gpu_init(int device);
+
+/* Release every resource the library holds (streams, staging, arenas). */
+void goofy_gpu_shutdown(void);
+
+/* Human-readable text for a status code. */
+const char* goofy_gpu_status_string(int status);
+
+/* Text of the last CUDA error the library saw on this thread ("" if none). */
+const char* goofy_gpu_last_error(void);
+
+/* ---- device pointers (asynchronous on `stream`) ---------------------------- */
+
+/* Device-pointer variant of goofy::compressDXT1 (goofy_tc.h:1497-1526).
+ * src: device RGBA8, `stride` bytes per row (4-byte aligned; 16-byte aligned
+ * src and stride take the vector-load path).  dst: device, 8-byte aligned,
+ * (width/4)*(height/4)*8 bytes.  width % 4 == 0 (not % 16: blocks are
+ * independent), height % 4 == 0.  Enqueues one kernel on `stream`; no sync. */
+int goofy_gpu_compress_bc1_device(void* dst, const void* src, uint32_t width, uint32_t height,
+                                  uint32_t stride, void* stream);
+
+/* Device-pointer variant of goofy::compressETC1 (goofy_tc.h:1528-1557). */
+int goofy_gpu_compress_etc1s_device(void* dst, const void* src, uint32_t width, uint32_t height,
+                                    uint32_t stride, void* stream);
+
+/* Either codec (GOOFY_CODEC_*). */
+int goofy_gpu_compress_device(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
+                              uint32_t stride, void* stream);
+
+/* ---- host pointers (synchronous, drop-in semantics) ------------------------ */
+
+/* Host-memory counterpart of goofy::compressDXT1 (goofy_tc.h:1497-1526): same
+ * arguments and output, returns when `dst` holds the result.  Pinned or
+ * pageable buffers of any alignment; width % 4 == 0, height % 4 == 0.  The
+ * image is streamed through the GPU in bands (copy in / encode / copy out
+ * overlapped on two streams).  Thread-safe (calls are serialised). */
+int goofy_gpu_compress_bc1_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
+                                uint32_t stride);
+
+/* Host-memory counterpart of goofy::compressETC1 (goofy_tc.h:1528-1557). */
+int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
+                                  uint32_t stride);
+
+int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
+                            uint32_t stride);
+
+/* ---- pinned host memory (for callers that want the fast host path) -------- */
+void* goofy_gpu_host_alloc(size_t bytes);
+void goofy_gpu_host_free(void* p);
+
+/* ---- tile shape (launch configuration of the image kernel) ---------------- */
+typedef struct goofy_gpu_tile {
+    uint32_t threads_per_cta;  /* 128, 256, 512 */
+    uint32_t blocks_per_thread; /* 1, 2, 4: 4x4 blocks one thread encodes per launch */
+} goofy_gpu_tile;
+
+/* Get / set the tile the image kernels launch with, per codec. */
+int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile);
+int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GOOFY_GPU_H */

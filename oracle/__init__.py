@@ -1,0 +1,68 @@
+"""Oracle package -- TEST INFRASTRUCTURE ONLY.
+
+``load()`` returns the ctypes handle of the C restatement (goofy_oracle.c);
+``load_ref()`` the reference encoder compiled from its own header (None where
+the reference tree is absent, e.g. on the GPU host).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU legs use these; the product
+package never imports this module.
+"""
+import ctypes
+import os
+
+from .build import ORACLE_SO, REF_SO
+
+_VP = ctypes.c_void_p
+_U = ctypes.c_uint
+_oracle = None
+_ref = None
+
+
+def load():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_SO):
+            from .build import build
+            build()
+        lib = ctypes.CDLL(ORACLE_SO)
+        lib.oracle_encode_block.restype = None
+        lib.oracle_encode_block.argtypes = [ctypes.c_int, _VP, ctypes.c_size_t, _VP]
+        for name in ("oracle_compress", "oracle_compress_any"):
+            fn = getattr(lib, name)
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U]
+        lib.oracle_compress_mt.restype = ctypes.c_int
+        lib.oracle_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
+        _oracle = lib
+    return _oracle
+
+
+def load_ref():
+    """The reference itself (x86-64 with the reference tree present), else None."""
+    global _ref
+    if _ref is None and os.path.exists(REF_SO):
+        lib = ctypes.CDLL(REF_SO)
+        lib.ref_compress.restype = ctypes.c_int
+        lib.ref_compress.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U]
+        lib.ref_compress_mt.restype = ctypes.c_int
+        lib.ref_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
+        _ref = lib
+    return _ref
+
+
+def encode(codec, img, width, height, stride=None, threads=1, any_width=True):
+    """Oracle output for an RGBA8 numpy image (rows of `stride` bytes)."""
+    import numpy as np
+
+    stride = stride or img.strides[0]
+    out = np.zeros((width // 4) * (height // 4) * 8, np.uint8)
+    lib = load()
+    if threads != 1:
+        rc = lib.oracle_compress_mt(codec, out.ctypes.data, img.ctypes.data, width, height, stride, threads)
+        rc = 0 if rc > 0 else rc
+    elif any_width:
+        rc = lib.oracle_compress_any(codec, out.ctypes.data, img.ctypes.data, width, height, stride)
+    else:
+        rc = lib.oracle_compress(codec, out.ctypes.data, img.ctypes.data, width, height, stride)
+    if rc != 0:
+        raise ValueError("oracle rejected the image: %d" % rc)
+    return out

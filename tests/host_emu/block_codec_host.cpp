@@ -1,0 +1,26 @@
+// block_codec_host.cpp -- TEST ONLY.  Compiles goofy_gb300/csrc/block_codec.cuh
+// for the CPU (through host_emulation.h) and exposes the per-block encoders
+// over a whole image, so tests can compare the kernel's arithmetic with the
+// oracle without a GPU.  Not linked into the library.
+#include <cstring>
+
+#include "block_codec.cuh"
+
+extern "C" int host_emu_encode(int codec, uint8_t* out, const uint8_t* src, unsigned width, unsigned height,
+                               unsigned stride)
+{
+    if (width % 4 || height % 4) return -1;
+    uint8_t lut[128];
+    for (uint32_t i = 0; i < 128; ++i) lut[i] = (uint8_t)goofy_gpu::etc_control_byte(2 * i);
+    const unsigned bw = width / 4, bh = height / 4;
+    for (unsigned by = 0; by < bh; ++by)
+        for (unsigned bx = 0; bx < bw; ++bx) {
+            uint32_t w[16];
+            for (int y = 0; y < 4; ++y)
+                std::memcpy(&w[4 * y], src + (size_t)(4 * by + y) * stride + 16 * (size_t)bx, 16);
+            uint2 r = codec == 0 ? goofy_gpu::encode_bc1(w) : goofy_gpu::encode_etc1s(w, lut);
+            std::memcpy(out + 8 * ((size_t)by * bw + bx), &r.x, 4);
+            std::memcpy(out + 8 * ((size_t)by * bw + bx) + 4, &r.y, 4);
+        }
+    return 0;
+}
