@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--soak-s", type=float, default=1.5, help="seconds of the same loop before the timed region "
                                                              "while clocks are sampled")
+    p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     return p.parse_args()
 
 
@@ -263,6 +265,28 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
 
+    names = {g.CODEC_BC1: "bc1", g.CODEC_ETC1S: "etc1s"}
+    tuned = {}
+    if args.sweep:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for c in codecs:
+            for threads, bpt, pers in [(t, b, p) for p in (0, 1) for t in (128, 256, 512) for b in (1, 2, 4)
+                                       if not (p and b == 4)]:
+                    g.set_tile(c, threads, bpt, pers)
+                    ts = []
+                    for r in range(9):
+                        e0.record(stream)
+                        g.compress_device(c, dst[c].data_ptr(), src[c].data_ptr(), W, H, 4 * W, sh)
+                        e1.record(stream)
+                        e1.synchronize()
+                        ts.append(e0.elapsed_time(e1) * 1e3)
+                    print("sweep %s threads=%d bpt=%d persistent=%d median_us=%.2f min_us=%.2f" % (
+                        names[c], threads, bpt, pers, statistics.median(ts), min(ts)), file=sys.stderr)
+    if not args.no_autotune:
+        for c in codecs:
+            tile, us = g.autotune(c, dst[c].data_ptr(), src[c].data_ptr(), W, H, 4 * W, reps=7)
+            tuned[names[c]] = {"tile": list(tile), "median_us": round(us, 2)}
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -335,7 +359,6 @@ def run_gpu(args):
         return 0
 
     peak, peak_kind = read_peaks()
-    names = {g.CODEC_BC1: "bc1", g.CODEC_ETC1S: "etc1s"}
     per_codec = {}
     for c in codecs:
         ms = statistics.mean(per_launch[c])
@@ -364,7 +387,7 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
-                       "tiles": tiles},
+                       "tiles": tiles, "autotune": tuned or None},
             "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}

@@ -45,7 +45,8 @@ _U32 = ctypes.c_uint32
 
 
 class Tile(ctypes.Structure):
-    _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32)]
+    _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
+                ("persistent", ctypes.c_uint32)]
 
 
 def _declare(lib):
@@ -64,6 +65,8 @@ def _declare(lib):
         "goofy_gpu_host_free": (None, [_VP]),
         "goofy_gpu_get_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
         "goofy_gpu_set_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
+        "goofy_gpu_autotune": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _U32, ctypes.POINTER(Tile),
+                                              ctypes.POINTER(ctypes.c_float)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -175,12 +178,24 @@ def get_tile(codec):
     rc = lib().goofy_gpu_get_tile(codec, ctypes.byref(t))
     if rc != OK:
         raise ValueError(status_string(rc))
-    return (t.threads_per_cta, t.blocks_per_thread)
+    return (t.threads_per_cta, t.blocks_per_thread, t.persistent)
 
 
-def set_tile(codec, threads_per_cta, blocks_per_thread):
-    t = Tile(threads_per_cta, blocks_per_thread)
+def set_tile(codec, threads_per_cta, blocks_per_thread, persistent=0):
+    t = Tile(threads_per_cta, blocks_per_thread, persistent)
     return lib().goofy_gpu_set_tile(codec, ctypes.byref(t))
+
+
+def autotune(codec, dst, src, width, height, stride, reps=9):
+    """Time every tile shape on a device image, install the fastest; returns
+    ((threads_per_cta, blocks_per_thread, persistent), median microseconds)."""
+    t = Tile()
+    us = ctypes.c_float()
+    rc = lib().goofy_gpu_autotune(codec, _addr(dst), _addr(src), width, height, stride, reps, ctypes.byref(t),
+                                  ctypes.byref(us))
+    if rc != OK:
+        raise RuntimeError("autotune failed: %s %s" % (status_string(rc), last_error()))
+    return (t.threads_per_cta, t.blocks_per_thread, t.persistent), us.value
 
 
 def out_size(width, height):

@@ -127,11 +127,11 @@ GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
     uint32_t idx = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {  // pixels i and i+8 share a register
-        const uint32_t s = perm(luma_sum(w[i], 0u), luma_sum(w[i + 8], 0u), 0x5410u);
+        const uint32_t s = luma_sum(w[i + 8], 0u) * 0x10000u + luma_sum(w[i], 0u);
         const uint32_t f_gez = s + k_gez, f_lo = s + k_lo, f_hi = s + k_hi;
         // bit 14: not gez, bit 15: lqt (and 30 / 31 for pixel i+8)
         const uint32_t z = (f_lo & ~f_hi & 0x80008000u) | (~f_gez & 0x40004000u);
-        idx += i < 7 ? __umulhi(z, 1u << (18 + 2 * i)) : z;  // z >> (14 - 2i)
+        idx = (idx >> 2) + z;  // after the last pair, pair i sits at bits 2i (and 16 + 2i)
     }
 
     // endpoints: lanes {max, min} for each channel, c0 in the low half
@@ -196,21 +196,34 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     const uint32_t word0 = (uint32_t)ctrl_lut[br.range >> 1] << 24 | rb5 << 3 | g5 << 11;
 
     // indices: bit j = not gez, bit 16+j = not lqt of the pixel with
-    // j = 4*(x^2) + y (transposeAs4x4x4 order, goofy_tc.h:1366-1395)
-    const uint32_t k_q = (0x8003u - 4u * br.mid) | (0x8003u - 4u * (br.mid - br.qt + 1u)) << 16;
-    const uint32_t k_h = (0x8003u - 4u * (br.mid + br.qt)) << 16;
-    uint32_t word1 = 0;
+    // j = 4*(x^2) + y (transposeAs4x4x4 order, goofy_tc.h:1366-1395).
+    // Per pixel, one register holds S + k in both 16-bit lanes (low lane: the
+    // gez test, high lane: the Y >= mid-qt+1 test) scaled by 2^m, so the flag
+    // bits land at 11+m / 27+m.  Pixels are grouped by the shift that still
+    // separates them from their final bit: j = 11..15 (m = j-11, no shift),
+    // j = 6..10 (m = j-6, >> 5), j = 1..5 (m = j-1, >> 10), j = 0 (>> 11);
+    // flags within a group are distinct bits, so groups are summed and
+    // shifted once.  Thresholds are clamped to [0, 1021], which keeps every
+    // lane value in [0, 4096) * 2^m without changing a test.
+    const uint32_t t_gez = min(max(4 * (int)br.mid - 3, 0), 1021);
+    const uint32_t t_lo = min(max(4 * ((int)br.mid - (int)br.qt) + 1, 0), 1021);
+    const uint32_t t_hi = min(4u * (br.mid + br.qt) - 3u, 1021u);
+    const uint32_t k_q = (2048u - t_gez) | (2048u - t_lo) << 16;
+    const uint32_t k_d = ((t_lo - t_hi) << 16) - (2048u - t_gez);  // q + k_d: low lane S, high lane S + 2048 - t_hi
+    uint32_t group[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int y = 0; y < 4; ++y)
 #pragma unroll
         for (int x = 0; x < 4; ++x) {
             const int j = 4 * (x ^ 2) + y;
+            const int gi = j >= 11 ? 0 : j >= 6 ? 1 : j >= 1 ? 2 : 3;
+            const int m = j >= 11 ? j - 11 : j >= 6 ? j - 6 : j >= 1 ? j - 1 : 0;
             const uint32_t s = luma_sum(w[4 * y + x], 0u);
-            const uint32_t q = s * 0x00010001u + k_q;  // bit 15: Y >= mid, bit 31: Y >= mid-qt+1
-            const uint32_t h = s * 0x00010000u + k_h;  // bit 31: Y >= mid+qt, bits 0..15 zero
-            const uint32_t z = (~q | h) & 0x80008000u;
-            word1 += j < 15 ? __umulhi(z, 1u << (17 + j)) : z;  // z >> (15 - j)
+            const uint32_t q = s * (0x00010001u << m) + (k_q << m);  // bit 11+m: Y >= mid, 27+m: Y >= mid-qt+1
+            const uint32_t h = q + (k_d << m);                        // bit 27+m: Y >= mid+qt; bit 11+m clear
+            group[gi] += (~q | h) & (0x08000800u << m);
         }
+    const uint32_t word1 = group[0] + (group[1] >> 5) + (group[2] >> 10) + (group[3] >> 11);
     return make_uint2(word0, word1);
 }
 

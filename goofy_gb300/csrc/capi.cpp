@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/goofy_gpu.h"
 #include "../../include/goofy_tc_gpu.h"
@@ -57,7 +58,7 @@ struct DeviceGuard {
     }
 };
 
-Tile g_tile[2] = {{256, 2}, {256, 2}};
+Tile g_tile[2] = {{256, 2, 0}, {256, 2, 0}};
 std::mutex g_tile_mu;
 
 Tile tile_for(int codec)
@@ -345,16 +346,84 @@ GOOFY_EXPORT int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile)
     const Tile t = tile_for(codec);
     tile->threads_per_cta = t.threads;
     tile->blocks_per_thread = t.bpt;
+    tile->persistent = t.persistent;
     return GOOFY_OK;
 }
 
 GOOFY_EXPORT int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile)
 {
     if (!tile || (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S)) return GOOFY_ERR_INVALID;
-    const Tile t{tile->threads_per_cta, tile->blocks_per_thread};
+    const Tile t{tile->threads_per_cta, tile->blocks_per_thread, tile->persistent};
     if (!goofy_gpu::tile_valid(t)) return GOOFY_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_tile_mu);
     g_tile[codec] = t;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
+                                   uint32_t stride, uint32_t reps, goofy_gpu_tile* best, float* best_us)
+{
+    int rc = check_args(codec, dst, src, width, height, stride);
+    if (rc <= 0) return rc == GOOFY_OK ? GOOFY_ERR_INVALID : rc;
+    if (reps == 0 || reps > 1000) return GOOFY_ERR_INVALID;
+    const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+    if (reinterpret_cast<uintptr_t>(dst) % 8 != 0 || s % 4 != 0 || stride % 4 != 0) return GOOFY_ERR_ALIGNMENT;
+    const SrcAccess access = (s % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int result = GOOFY_OK;
+    Tile best_tile{0, 0, 0};
+    float best_time = 0.f;
+    std::vector<float> times(reps);
+    for (int i = 0; i < 2 && result == GOOFY_OK; ++i)
+        if (cudaEventCreate(&ev[i]) != cudaSuccess) result = cuda_fail(cudaGetLastError(), "cudaEventCreate");
+    std::vector<Tile> candidates;
+    for (uint32_t persistent : {0u, 1u})
+        for (uint32_t threads : {128u, 256u, 512u})
+            for (uint32_t bpt : {1u, 2u, 4u})
+                if (goofy_gpu::tile_valid(Tile{threads, bpt, persistent}))
+                    candidates.push_back(Tile{threads, bpt, persistent});
+    for (const Tile& t : candidates) {
+        if (result != GOOFY_OK) break;
+        auto launch = [&] {
+            return goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
+                                           width, height, t, access, st);
+        };
+        cudaError_t e = cudaSuccess;
+        for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = launch();
+        for (uint32_t r = 0; r < reps && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(ev[0], st);
+            if (e == cudaSuccess) e = launch();
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&times[r], ev[0], ev[1]);
+        }
+        if (e != cudaSuccess) {
+            result = cuda_fail(e, "autotune launch");
+            break;
+        }
+        std::sort(times.begin(), times.end());
+        const float med = times[reps / 2];
+        if (best_tile.threads == 0 || med < best_time) {
+            best_time = med;
+            best_tile = t;
+        }
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(st);
+    if (result != GOOFY_OK) return result;
+    {
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        g_tile[codec] = best_tile;
+    }
+    if (best) {
+        best->threads_per_cta = best_tile.threads;
+        best->blocks_per_thread = best_tile.bpt;
+        best->persistent = best_tile.persistent;
+    }
+    if (best_us) *best_us = best_time * 1e3f;
     return GOOFY_OK;
 }
 

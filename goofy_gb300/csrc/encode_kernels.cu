@@ -64,46 +64,143 @@ __device__ __forceinline__ void fill_ctrl_lut(uint8_t* lut)
     for (uint32_t i = threadIdx.x; i < 128; i += blockDim.x) lut[i] = (uint8_t)etc_control_byte(2 * i);
 }
 
+// n / d for n < 2^32 with magic = floor((2^32 - 1) / d): the estimate is low
+// by at most one.
+__device__ __forceinline__ uint32_t div_magic(uint32_t n, uint32_t d, uint32_t magic, uint32_t& rem)
+{
+    uint32_t q = __umulhi(n, magic);
+    uint32_t r = n - q * d;
+    if (r >= d) {
+        ++q;
+        r -= d;
+    }
+    rem = r;
+    return q;
+}
+
+struct Segment {
+    uint32_t by, bx0;  // block row, first block of this lane
+};
+
+template <int BPT, SrcAccess ACCESS>
+__device__ __forceinline__ Segment load_segment(const uint8_t* __restrict__ src, size_t stride, uint32_t bw,
+                                                uint32_t seg, uint32_t segs_per_row, uint32_t seg_magic,
+                                                uint32_t lane, uint32_t (&w)[BPT][16])
+{
+    uint32_t sx;
+    Segment sg;
+    sg.by = div_magic(seg, segs_per_row, seg_magic, sx);
+    sg.bx0 = sx * (32u * BPT) + lane;
+    const uint8_t* row = src + (size_t)sg.by * 4u * stride;
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t bx = sg.bx0 + 32u * j;
+        if (bx < bw) load_block<ACCESS>(row + 16u * (size_t)bx, stride, w[j]);
+    }
+    return sg;
+}
+
+template <int CODEC, int BPT>
+__device__ __forceinline__ void encode_segment(uint8_t* __restrict__ dst, uint32_t bw, Segment sg,
+                                               const uint32_t (&w)[BPT][16], const uint8_t* ctrl_lut)
+{
+    uint8_t* out = dst + (size_t)sg.by * bw * 8u;
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t bx = sg.bx0 + 32u * j;
+        if (bx < bw) st_stream8(out + 8u * (size_t)bx, encode_block<CODEC>(w[j], ctrl_lut));
+    }
+}
+
+// Persistent grid: warp-segments are dealt round-robin to the resident warps;
+// each warp loads its next segment before encoding the current one, so the
+// 64*BPT bytes per lane of the next segment are in flight during the math.
+// One segment per warp: every lane issues its 4*BPT row loads up front.
 template <int CODEC, int BPT, SrcAccess ACCESS>
 __global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __restrict__ src, size_t stride,
-                                                           uint8_t* __restrict__ dst, uint32_t bw, uint32_t bh,
-                                                           uint32_t segs_per_row)
+                                                           uint8_t* __restrict__ dst, uint32_t bw,
+                                                           uint32_t total_segs, uint32_t segs_per_row,
+                                                           uint32_t seg_magic)
 {
     __shared__ uint8_t ctrl_lut[128];
     if constexpr (CODEC == kETC1S) {
         fill_ctrl_lut(ctrl_lut);
         __syncthreads();
     }
-    const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const uint32_t by = warp / segs_per_row;
-    if (by >= bh) return;
-    const uint32_t bx0 = (warp - by * segs_per_row) * (32u * BPT) + (threadIdx.x & 31u);
-    const uint8_t* row = src + (size_t)by * 4u * stride;
-
+    const uint32_t seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (seg >= total_segs) return;
     uint32_t w[BPT][16];
-#pragma unroll
-    for (int j = 0; j < BPT; ++j) {
-        const uint32_t bx = bx0 + 32u * j;
-        if (bx < bw) load_block<ACCESS>(row + 16u * (size_t)bx, stride, w[j]);
+    const Segment sg = load_segment<BPT, ACCESS>(src, stride, bw, seg, segs_per_row, seg_magic, threadIdx.x & 31u, w);
+    encode_segment<CODEC, BPT>(dst, bw, sg, w, ctrl_lut);
+}
+
+template <int CODEC, int BPT, SrcAccess ACCESS>
+__global__ void __launch_bounds__(512) encode_image_persistent(const uint8_t* __restrict__ src, size_t stride,
+                                                               uint8_t* __restrict__ dst, uint32_t bw,
+                                                               uint32_t total_segs, uint32_t segs_per_row,
+                                                               uint32_t seg_magic)
+{
+    __shared__ uint8_t ctrl_lut[128];
+    if constexpr (CODEC == kETC1S) {
+        fill_ctrl_lut(ctrl_lut);
+        __syncthreads();
     }
-    uint8_t* out = dst + (size_t)by * bw * 8u;
-#pragma unroll
-    for (int j = 0; j < BPT; ++j) {
-        const uint32_t bx = bx0 + 32u * j;
-        if (bx < bw) st_stream8(out + 8u * (size_t)bx, encode_block<CODEC>(w[j], ctrl_lut));
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp_stride = gridDim.x * (blockDim.x >> 5);
+    uint32_t seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    uint32_t a[BPT][16], b[BPT][16];
+    Segment sa{}, sb{};
+    if (seg < total_segs) sa = load_segment<BPT, ACCESS>(src, stride, bw, seg, segs_per_row, seg_magic, lane, a);
+    while (seg < total_segs) {
+        uint32_t next = seg + warp_stride;
+        if (next < total_segs) sb = load_segment<BPT, ACCESS>(src, stride, bw, next, segs_per_row, seg_magic, lane, b);
+        encode_segment<CODEC, BPT>(dst, bw, sa, a, ctrl_lut);
+        seg = next;
+        if (seg >= total_segs) break;
+        next = seg + warp_stride;
+        if (next < total_segs) sa = load_segment<BPT, ACCESS>(src, stride, bw, next, segs_per_row, seg_magic, lane, a);
+        encode_segment<CODEC, BPT>(dst, bw, sb, b, ctrl_lut);
+        seg = next;
     }
 }
 
 template <int CODEC, int BPT, SrcAccess ACCESS>
+static int resident_ctas(uint32_t threads)
+{
+    // cached per instantiation and block size (the device is the current one)
+    static int cached[3] = {0, 0, 0};
+    const int slot = threads == 128 ? 0 : threads == 256 ? 1 : 2;
+    if (cached[slot] == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_persistent<CODEC, BPT, ACCESS>, threads, 0);
+        cached[slot] = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    return cached[slot];
+}
+
+template <int CODEC, int BPT, SrcAccess ACCESS>
 static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
-                            uint32_t threads, cudaStream_t stream)
+                            uint32_t threads, bool persistent, cudaStream_t stream)
 {
     const uint32_t segs = (bw + 32u * BPT - 1) / (32u * BPT);
-    const uint64_t warps = (uint64_t)segs * bh;
+    const uint64_t total = (uint64_t)segs * bh;
+    if (total > 0x7fffffffull) return cudaErrorInvalidValue;
     const uint32_t wpc = threads / 32u;
-    const uint64_t ctas = (warps + wpc - 1) / wpc;
-    if (ctas > 0x7fffffffull) return cudaErrorInvalidConfiguration;
-    encode_image_kernel<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(src, stride, dst, bw, bh, segs);
+    uint64_t ctas = (total + wpc - 1) / wpc;
+    const uint32_t magic = 0xffffffffu / segs;
+    if constexpr (BPT <= 2) {
+        if (persistent) {
+            const uint64_t resident = (uint64_t)resident_ctas<CODEC, BPT, ACCESS>(threads);
+            if (ctas > resident) ctas = resident;
+            encode_image_persistent<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(
+                src, stride, dst, bw, (uint32_t)total, segs, magic);
+            return cudaGetLastError();
+        }
+    }
+    encode_image_kernel<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(src, stride, dst, bw,
+                                                                                   (uint32_t)total, segs, magic);
     return cudaGetLastError();
 }
 
@@ -112,9 +209,9 @@ static cudaError_t launch_bpt(const uint8_t* src, size_t stride, uint8_t* dst, u
                               cudaStream_t stream)
 {
     switch (tile.bpt) {
-    case 1: return launch_t<CODEC, 1, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
-    case 2: return launch_t<CODEC, 2, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
-    case 4: return launch_t<CODEC, 4, ACCESS>(src, stride, dst, bw, bh, tile.threads, stream);
+    case 1: return launch_t<CODEC, 1, ACCESS>(src, stride, dst, bw, bh, tile.threads, tile.persistent, stream);
+    case 2: return launch_t<CODEC, 2, ACCESS>(src, stride, dst, bw, bh, tile.threads, tile.persistent, stream);
+    case 4: return launch_t<CODEC, 4, ACCESS>(src, stride, dst, bw, bh, tile.threads, false, stream);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -9,13 +9,16 @@
 namespace goofy_gpu {
 
 struct Tile {
-    uint32_t threads;  // threads per CTA: 128, 256 or 512
-    uint32_t bpt;      // 4x4 blocks per thread: 1, 2 or 4
+    uint32_t threads;     // threads per CTA: 128, 256 or 512
+    uint32_t bpt;         // 4x4 blocks per thread and segment: 1, 2 or 4 (1 or 2 when persistent)
+    uint32_t persistent;  // 0: one segment per warp; 1: resident grid looping over segments with prefetch
 };
 
 inline bool tile_valid(const Tile& t)
 {
-    return (t.threads == 128 || t.threads == 256 || t.threads == 512) && (t.bpt == 1 || t.bpt == 2 || t.bpt == 4);
+    if (t.threads != 128 && t.threads != 256 && t.threads != 512) return false;
+    if (t.persistent > 1) return false;
+    return t.bpt == 1 || t.bpt == 2 || (t.bpt == 4 && !t.persistent);
 }
 
 // How the image kernel reads its source rows.

@@ -92,13 +92,22 @@ void goofy_gpu_host_free(void* p);
 
 /* ---- tile shape (launch configuration of the image kernel) ---------------- */
 typedef struct goofy_gpu_tile {
-    uint32_t threads_per_cta;  /* 128, 256, 512 */
-    uint32_t blocks_per_thread; /* 1, 2, 4: 4x4 blocks one thread encodes per launch */
+    uint32_t threads_per_cta;   /* 128, 256, 512 */
+    uint32_t blocks_per_thread; /* 4x4 blocks a thread encodes per segment: 1, 2, 4 (1, 2 if persistent) */
+    uint32_t persistent;        /* 0: one segment per warp; 1: resident grid, loop with prefetch */
 } goofy_gpu_tile;
 
 /* Get / set the tile the image kernels launch with, per codec. */
 int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile);
 int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
+
+/* Autotuner: times every tile shape on the caller's device image (`src`,
+ * `dst` as for goofy_gpu_compress_device, on the current device) with CUDA
+ * events -- `reps` timed launches per shape after two warm-up launches, median
+ * kept -- installs the fastest as the codec's tile and returns it with its
+ * median launch time in microseconds.  Synchronous.  No reference counterpart. */
+int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
+                       uint32_t reps, goofy_gpu_tile* best, float* best_us);
 
 #ifdef __cplusplus
 }

@@ -69,8 +69,11 @@ def test_c_abi_argument_checks(built):
 def test_tile_get_set(built):
     for codec in (0, 1):
         before = g.get_tile(codec)
-        assert g.set_tile(codec, 512, 4) == g.OK
-        assert g.get_tile(codec) == (512, 4)
+        assert g.set_tile(codec, 512, 2, 1) == g.OK
+        assert g.get_tile(codec) == (512, 2, 1)
+        assert g.set_tile(codec, 256, 4, 0) == g.OK
+        assert g.set_tile(codec, 256, 4, 1) == g.ERR_INVALID
+        assert g.set_tile(codec, 256, 2, 2) == g.ERR_INVALID
         assert g.set_tile(codec, 96, 2) == g.ERR_INVALID
         assert g.set_tile(codec, 256, 3) == g.ERR_INVALID
         assert g.set_tile(codec, *before) == g.OK

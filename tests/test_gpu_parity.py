@@ -15,7 +15,7 @@ from goofy_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 CODECS = [("bc1", g.CODEC_BC1), ("etc1s", g.CODEC_ETC1S)]
-TILES = [(t, b) for t in (128, 256, 512) for b in (1, 2, 4)]
+TILES = [(t, b, p) for p in (0, 1) for t in (128, 256, 512) for b in (1, 2, 4) if not (p and b == 4)]
 GUARD = 256
 
 
@@ -64,7 +64,7 @@ def test_ragged_sizes(cuda, name, codec, w, h):
     rng = np.random.default_rng(w * 1000 + h)
     img = rng.integers(0, 256, (h, 4 * w), dtype=np.uint8)
     want = oracle.encode(codec, img, w, h)
-    for tile in ((256, 1), (128, 4)):
+    for tile in ((256, 1, 0), (128, 4, 0), (256, 2, 1)):
         np.testing.assert_array_equal(device_encode(cuda, codec, img, w, h, tile=tile), want)
 
 
