@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--soak-s", type=float, default=1.5, help="seconds of the same loop before the timed region "
                                                              "while clocks are sampled")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     return p.parse_args()
 
@@ -185,6 +187,80 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
             "single_thread_mpix_s": round(px / t1 / 1e6, 1),
             "median_mpix_s": round(px / statistics.median(times) / 1e6, 1),
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
+
+
+def run_batched(args, g, torch, stream, dev):
+    """Mixed batch: `--batch-textures` textures (64..2048 per side, 20% with
+    mip chains, BC1 / ETC1s 50/50), every level resident in HBM.  Batched =
+    one persistent launch per step (autotuned tile, CUDA-graph replay); plain
+    = one image-kernel launch per texture level, back to back on one stream."""
+    import numpy as np
+
+    from goofy_gb300 import workloads
+
+    t0 = time.perf_counter()
+    levels = workloads.texture_batch(args.batch_textures)
+    gen_s = time.perf_counter() - t0
+    pixels = sum(lv["width"] * lv["height"] for lv in levels)
+    in_bytes = sum((lv["pixels"].size + 255) // 256 * 256 for lv in levels)
+    out_sizes = [g.out_size(lv["width"], lv["height"]) for lv in levels]
+    arena_in = torch.empty(in_bytes, dtype=torch.uint8, device=dev)
+    outs = [torch.zeros(sum(out_sizes), dtype=torch.uint8, device=dev) for _ in range(2)]
+    descs = [[], []]
+    off_in = off_out = 0
+    for lv, n in zip(levels, out_sizes):
+        px = lv["pixels"]
+        arena_in[off_in:off_in + px.size] = torch.from_numpy(np.ascontiguousarray(px).reshape(-1)).to(dev)
+        for k in range(2):
+            descs[k].append((arena_in.data_ptr() + off_in, outs[k].data_ptr() + off_out, lv["width"], lv["height"],
+                             px.strides[0], lv["codec"]))
+        off_in += (px.size + 255) // 256 * 256
+        off_out += n
+    sh = stream.cuda_stream
+    reps = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def plain_pass(k):
+        for d in descs[k]:
+            rc = g.compress_device(d[5], d[1], d[0], d[2], d[3], d[4], sh)
+            if rc != g.OK:
+                raise RuntimeError(g.last_error())
+
+    plain_pass(0)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        plain_pass(0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / reps
+    plain_launches = len(descs[0])
+
+    b = g.Batch(len(levels), torch.cuda.current_device())
+    try:
+        arr = g.images_array(descs[1])
+        tile, tuned_us = b.autotune(arr, reps=3)
+        for _ in range(3):
+            assert b.encode(arr, sh) == g.OK, g.last_error()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            b.encode(arr, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        batch_ms = e0.elapsed_time(e1) / reps
+    finally:
+        b.close()
+    exact = bool(torch.equal(outs[0], outs[1]))
+    return {"workload": "%d textures, 64..2048 px per side (log-uniform), 20%% with full mip chains, "
+                        "BC1/ETC1s 50/50, content = synthetic scene seeded by texture index" % args.batch_textures,
+            "levels": len(levels), "pixels": pixels, "generate_s": round(gen_s, 1),
+            "batched_mpix_s": round(pixels / (batch_ms / 1e3) / 1e6, 1), "batched_ms": round(batch_ms, 4),
+            "batched_hbm_gbs": round(ALG_BYTES_PER_PX * pixels / (batch_ms / 1e3) / 1e9, 1),
+            "batched_tile": list(tile), "plain_mpix_s": round(pixels / (plain_ms / 1e3) / 1e6, 1),
+            "plain_ms": round(plain_ms, 4), "plain_launches_per_step": plain_launches,
+            "speedup_vs_plain": round(plain_ms / batch_ms, 2), "bit_exact_vs_plain": exact,
+            "graphs": True}
 
 
 def run_reference(args):
@@ -376,6 +452,9 @@ def run_gpu(args):
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s"}
     cpu = None
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, g, torch, stream, dev)
     if not args.no_cpu:
         from oracle import build as oracle_build
 
@@ -388,7 +467,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
     print(json.dumps(line), flush=True)

@@ -49,6 +49,17 @@ class Tile(ctypes.Structure):
                 ("persistent", ctypes.c_uint32)]
 
 
+class Image(ctypes.Structure):
+    """goofy_gpu_image: one device image of a batch."""
+    _fields_ = [("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("stride", ctypes.c_uint32), ("codec", ctypes.c_int32)]
+
+
+class BatchTile(ctypes.Structure):
+    _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
+                ("unit_blocks", ctypes.c_uint32)]
+
+
 def _declare(lib):
     sigs = {
         "goofy_gpu_init": (ctypes.c_int, [ctypes.c_int]),
@@ -67,6 +78,14 @@ def _declare(lib):
         "goofy_gpu_set_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
         "goofy_gpu_autotune": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _U32, ctypes.POINTER(Tile),
                                               ctypes.POINTER(ctypes.c_float)]),
+        "goofy_gpu_batch_create": (ctypes.c_int, [ctypes.POINTER(_VP), _U32, ctypes.c_int]),
+        "goofy_gpu_batch_destroy": (None, [_VP]),
+        "goofy_gpu_batch_encode": (ctypes.c_int, [_VP, ctypes.POINTER(Image), _U32, _VP]),
+        "goofy_gpu_batch_set_graphs": (ctypes.c_int, [_VP, ctypes.c_int]),
+        "goofy_gpu_batch_get_tile": (ctypes.c_int, [_VP, ctypes.POINTER(BatchTile)]),
+        "goofy_gpu_batch_set_tile": (ctypes.c_int, [_VP, ctypes.POINTER(BatchTile)]),
+        "goofy_gpu_batch_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Image), _U32, _U32, ctypes.POINTER(BatchTile),
+                                                    ctypes.POINTER(ctypes.c_float)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -201,3 +220,58 @@ def autotune(codec, dst, src, width, height, stride, reps=9):
 def out_size(width, height):
     """Bytes of encoded output: (width/4)*(height/4) blocks of 8 bytes."""
     return (width // 4) * (height // 4) * 8
+
+
+def images_array(images):
+    """ctypes array of Image from (src, dst, width, height, stride, codec) tuples or Image objects."""
+    arr = (Image * len(images))()
+    for i, im in enumerate(images):
+        arr[i] = im if isinstance(im, Image) else Image(_addr(im[0]), _addr(im[1]), *im[2:])
+    return arr
+
+
+class Batch:
+    """goofy_gpu_batch: many device images of uneven sizes per persistent launch."""
+
+    def __init__(self, max_images, device=0):
+        h = ctypes.c_void_p()
+        rc = lib().goofy_gpu_batch_create(ctypes.byref(h), max_images, device)
+        if rc != OK:
+            raise RuntimeError("goofy_gpu_batch_create: %s %s" % (status_string(rc), last_error()))
+        self._h = h
+
+    def encode(self, images, stream=None):
+        arr = images if isinstance(images, ctypes.Array) else images_array(images)
+        return lib().goofy_gpu_batch_encode(self._h, arr, len(arr), stream)
+
+    def set_graphs(self, enable):
+        return lib().goofy_gpu_batch_set_graphs(self._h, 1 if enable else 0)
+
+    def get_tile(self):
+        t = BatchTile()
+        assert lib().goofy_gpu_batch_get_tile(self._h, ctypes.byref(t)) == OK
+        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks)
+
+    def set_tile(self, threads_per_cta, blocks_per_thread, unit_blocks):
+        t = BatchTile(threads_per_cta, blocks_per_thread, unit_blocks)
+        return lib().goofy_gpu_batch_set_tile(self._h, ctypes.byref(t))
+
+    def autotune(self, images, reps=5):
+        arr = images if isinstance(images, ctypes.Array) else images_array(images)
+        t = BatchTile()
+        us = ctypes.c_float()
+        rc = lib().goofy_gpu_batch_autotune(self._h, arr, len(arr), reps, ctypes.byref(t), ctypes.byref(us))
+        if rc != OK:
+            raise RuntimeError("batch autotune: %s %s" % (status_string(rc), last_error()))
+        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks), us.value
+
+    def close(self):
+        if self._h:
+            lib().goofy_gpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

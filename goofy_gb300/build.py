@@ -34,9 +34,9 @@ def _cuda_home():
     return os.path.dirname(os.path.dirname(_nvcc()))
 
 
-CU_SOURCES = ["encode_kernels.cu"]
-CPP_SOURCES = ["capi.cpp"]
-HEADERS = ["block_codec.cuh", "kernels.h"]
+CU_SOURCES = ["encode_kernels.cu", "batch_kernels.cu"]
+CPP_SOURCES = ["capi.cpp", "batch.cpp"]
+HEADERS = ["block_codec.cuh", "device_io.cuh", "kernels.h", "batch.h", "host_util.h"]
 
 
 def _stale(target, deps):

@@ -18,16 +18,14 @@
 
 #include "../../include/goofy_gpu.h"
 #include "../../include/goofy_tc_gpu.h"
+#include "host_util.h"
 #include "kernels.h"
 
-#define GOOFY_EXPORT __attribute__((visibility("default")))
+namespace goofy_gpu {
 
 namespace {
-
-using goofy_gpu::SrcAccess;
-using goofy_gpu::Tile;
-
 thread_local char g_last_error[256] = "";
+}
 
 int cuda_fail(cudaError_t e, const char* what)
 {
@@ -37,26 +35,24 @@ int cuda_fail(cudaError_t e, const char* what)
                                                                            : GOOFY_ERR_CUDA;
 }
 
-#define CUDA_TRY(call)                                        \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
-    } while (0)
+int fail(int status, const char* what)
+{
+    std::snprintf(g_last_error, sizeof g_last_error, "%s", what);
+    return status;
+}
 
-// Restores the caller's current device on scope exit.
-struct DeviceGuard {
-    int prev = -1;
-    cudaError_t err = cudaSuccess;
-    explicit DeviceGuard(int dev)
-    {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) err = cudaSetDevice(dev);
-    }
-    ~DeviceGuard()
-    {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
+const char* last_error_text() { return g_last_error; }
+
+}  // namespace goofy_gpu
+
+namespace {
+
+using goofy_gpu::cuda_fail;
+using goofy_gpu::DeviceGuard;
+using goofy_gpu::SrcAccess;
+using goofy_gpu::Tile;
+
+#define CUDA_TRY GOOFY_CUDA_TRY
 
 Tile g_tile[2] = {{256, 2, 0}, {256, 2, 0}};
 std::mutex g_tile_mu;
@@ -287,7 +283,7 @@ GOOFY_EXPORT const char* goofy_gpu_status_string(int status)
     }
 }
 
-GOOFY_EXPORT const char* goofy_gpu_last_error(void) { return g_last_error; }
+GOOFY_EXPORT const char* goofy_gpu_last_error(void) { return goofy_gpu::last_error_text(); }
 
 GOOFY_EXPORT int goofy_gpu_compress_device(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
                                            uint32_t stride, void* stream)

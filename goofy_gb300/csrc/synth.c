@@ -19,6 +19,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #define EXPORT __attribute__((visibility("default")))
 
@@ -120,26 +121,92 @@ typedef struct {
     const noise_field* nf;
 } scene_rows;
 
+/* Per-column lattice index and smoothed weight of each octave: the same
+ * expressions noise_at() evaluates, computed once per column. */
+typedef struct {
+    unsigned* i;
+    double* t;
+} axis_weights;
+
+static int axis_init(axis_weights* a, const noise_field* nf, unsigned n)
+{
+    a->i = (unsigned*)malloc(sizeof(unsigned) * 4 * (size_t)n);
+    a->t = (double*)malloc(sizeof(double) * 4 * (size_t)n);
+    if (!a->i || !a->t) return -1;
+    for (int o = 0; o < 4; ++o) {
+        const unsigned p = (unsigned)nf->oct[o].period;
+        for (unsigned x = 0; x < n; ++x) {
+            a->i[(size_t)o * n + x] = x / p;
+            a->t[(size_t)o * n + x] = smooth((double)(x % p) / (double)p);
+        }
+    }
+    return 0;
+}
+
+static void axis_free(axis_weights* a)
+{
+    free(a->i);
+    free(a->t);
+}
+
 static void* scene_rows_main(void* arg)
 {
     const scene_rows* s = (const scene_rows*)arg;
     const double sx = s->w > 1 ? 255.0 / (double)(s->w - 1) : 0.0;
     const double sy = s->h > 1 ? 255.0 / (double)(s->h - 1) : 0.0;
     const double sb = (s->w + s->h) > 2 ? 255.0 / (double)(s->w + s->h - 2) : 0.0;
+    axis_weights ax;
+    if (axis_init(&ax, s->nf, s->w) != 0) {
+        axis_free(&ax);
+        /* fall back to the direct evaluation */
+        for (unsigned y = s->y0; y < s->y1; ++y) {
+            uint8_t* row = s->dst + (size_t)y * s->stride;
+            for (unsigned x = 0; x < s->w; ++x) {
+                const double base[3] = {(double)x * sx, (double)y * sy, (double)(x + y) * sb};
+                for (int c = 0; c < 3; ++c) row[4 * x + c] = clamp_round(base[c] + noise_at(s->nf, c, x, y));
+                row[4 * x + 3] = 255;
+            }
+        }
+        return NULL;
+    }
     for (unsigned y = s->y0; y < s->y1; ++y) {
         uint8_t* row = s->dst + (size_t)y * s->stride;
+        unsigned jy[4];
+        double ty[4];
+        for (int o = 0; o < 4; ++o) {
+            const unsigned p = (unsigned)s->nf->oct[o].period;
+            jy[o] = y / p;
+            ty[o] = smooth((double)(y % p) / (double)p);
+        }
         for (unsigned x = 0; x < s->w; ++x) {
             const double base[3] = {(double)x * sx, (double)y * sy, (double)(x + y) * sb};
-            for (int c = 0; c < 3; ++c) row[4 * x + c] = clamp_round(base[c] + noise_at(s->nf, c, x, y));
+            for (int c = 0; c < 3; ++c) {
+                double v = 0.0;
+                for (int o = 0; o < 4; ++o) {
+                    const octave* oc = &s->nf->oct[o];
+                    const unsigned i = ax.i[(size_t)o * s->w + x];
+                    const double tx = ax.t[(size_t)o * s->w + x];
+                    const double* L = oc->lattice + (size_t)c * oc->gw * oc->gh;
+                    const double a = L[(size_t)jy[o] * oc->gw + i], b = L[(size_t)jy[o] * oc->gw + i + 1];
+                    const double d = L[(size_t)(jy[o] + 1) * oc->gw + i], e = L[(size_t)(jy[o] + 1) * oc->gw + i + 1];
+                    const double top = a + (b - a) * tx, bot = d + (e - d) * tx;
+                    v += oc->amp * (top + (bot - top) * ty[o]);
+                }
+                row[4 * x + c] = clamp_round(base[c] + v);
+            }
             row[4 * x + 3] = 255;
         }
     }
+    axis_free(&ax);
     return NULL;
 }
 
 static void run_rows(scene_rows* proto, int threads)
 {
-    if (threads < 1) threads = 1;
+    if (threads < 1) {  /* 0: one per online CPU */
+        long n = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = n > 0 ? (int)n : 1;
+    }
     if ((unsigned)threads > proto->h) threads = proto->h ? (int)proto->h : 1;
     pthread_t tid[64];
     scene_rows part[64];

@@ -109,6 +109,49 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
 
+/* ---- batches: many device images of uneven sizes in one launch ----------- */
+
+/* One image of a batch (a texture or one of its mip levels).  src / dst and
+ * the size rules are those of goofy_gpu_compress_device; codec per image. */
+typedef struct goofy_gpu_image {
+    const void* src;
+    void* dst;
+    uint32_t width, height, stride;
+    int32_t codec; /* GOOFY_CODEC_* */
+} goofy_gpu_image;
+
+typedef struct goofy_gpu_batch goofy_gpu_batch;
+
+typedef struct goofy_gpu_batch_tile {
+    uint32_t threads_per_cta;   /* 128, 256, 512 */
+    uint32_t blocks_per_thread; /* 1 or 2 */
+    uint32_t unit_blocks;       /* 4x4 blocks per work unit, a multiple of 32 * blocks_per_thread */
+} goofy_gpu_batch_tile;
+
+/* A batch object for up to `max_images` images per call on `device`; owns its
+ * descriptor tables, work counters, stream and graphs.  No reference
+ * counterpart (the reference encodes one image per call). */
+int goofy_gpu_batch_create(goofy_gpu_batch** batch, uint32_t max_images, int device);
+void goofy_gpu_batch_destroy(goofy_gpu_batch* batch);
+
+/* Encode `count` images in one persistent launch: warps pull work units
+ * (runs of unit_blocks blocks of one image) from a device work counter.
+ * Asynchronous: ordered after the work already queued on `stream`, and later
+ * work on `stream` waits for it.  Each image's output equals
+ * goofy_gpu_compress_device on that image alone. */
+int goofy_gpu_batch_encode(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, void* stream);
+
+/* CUDA-graph replay of same-shaped batches (default on). */
+int goofy_gpu_batch_set_graphs(goofy_gpu_batch* batch, int enable);
+int goofy_gpu_batch_get_tile(goofy_gpu_batch* batch, goofy_gpu_batch_tile* tile);
+int goofy_gpu_batch_set_tile(goofy_gpu_batch* batch, const goofy_gpu_batch_tile* tile);
+
+/* Time every batch tile on this set of images (CUDA events, `reps` timed
+ * launches each, median), keep the fastest for this batch object.  Writes
+ * the images' outputs as a side effect.  Synchronous. */
+int goofy_gpu_batch_autotune(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, uint32_t reps,
+                             goofy_gpu_batch_tile* best, float* best_us);
+
 #ifdef __cplusplus
 }
 #endif
