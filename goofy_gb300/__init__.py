@@ -35,6 +35,7 @@ ERR_TOO_LARGE = -10
 
 CODEC_BC1 = 0
 CODEC_ETC1S = 1
+NOALLOC_MAX_IMAGES = 256
 CODECS = {"bc1": CODEC_BC1, "dxt1": CODEC_BC1, "etc1s": CODEC_ETC1S, "etc1": CODEC_ETC1S}
 
 _lib = None
@@ -86,6 +87,7 @@ def _declare(lib):
         "goofy_gpu_batch_set_tile": (ctypes.c_int, [_VP, ctypes.POINTER(BatchTile)]),
         "goofy_gpu_batch_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Image), _U32, _U32, ctypes.POINTER(BatchTile),
                                                     ctypes.POINTER(ctypes.c_float)]),
+        "goofy_gpu_batch_encode_noalloc": (ctypes.c_int, [ctypes.POINTER(Image), _U32, _VP]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -275,3 +277,11 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def batch_encode_noalloc(images, stream=None):
+    """goofy_gpu_batch_encode_noalloc: a batch of at most NOALLOC_MAX_IMAGES
+    images encoded without any allocation (scratch in a fixed device array of
+    the library; calls sharing it must not overlap on the GPU)."""
+    arr = images if isinstance(images, ctypes.Array) else images_array(images)
+    return lib().goofy_gpu_batch_encode_noalloc(arr, len(arr), stream)

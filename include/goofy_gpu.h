@@ -152,6 +152,29 @@ int goofy_gpu_batch_set_tile(goofy_gpu_batch* batch, const goofy_gpu_batch_tile*
 int goofy_gpu_batch_autotune(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, uint32_t reps,
                              goofy_gpu_batch_tile* best, float* best_us);
 
+/* ---- batch encoding without any allocation ---------------------------------- */
+
+/* Largest image count goofy_gpu_batch_encode_noalloc takes per call. */
+#define GOOFY_NOALLOC_MAX_IMAGES 256
+
+/* Encodes a batch like goofy_gpu_batch_encode (same images, same output) but
+ * allocates nothing, for callers that may not call cudaMalloc / cudaFree or
+ * any allocating routine while they encode -- e.g. a texture-streaming thread
+ * inside a renderer's frame budget, where the CUDA allocator can stall the
+ * device, or an engine whose own allocator owns all GPU memory.  No
+ * counterpart in the reference.
+ * The work counter and descriptor tables live in one fixed file-scope device
+ * array of the library (13,568 bytes, held on every GPU that loads the library
+ * until the process exits), so a call takes at most GOOFY_NOALLOC_MAX_IMAGES
+ * images; more returns GOOFY_ERR_TOO_LARGE.  The caller's images (device
+ * src / dst) are the inputs and outputs.  The first call on a device looks up
+ * the array's device address with cudaGetSymbolAddress; make that first call
+ * before any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps (e.g. on two unordered streams) race; issue them on one stream or
+ * order them.  Asynchronous on `stream` (the descriptor copy is staged from
+ * the calling thread's stack before the function returns). */
+int goofy_gpu_batch_encode_noalloc(const goofy_gpu_image* images, uint32_t count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
