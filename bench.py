@@ -51,6 +51,8 @@ def parse():
                                                              "while clocks are sampled")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--serve-seconds", type=float, default=1.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     return p.parse_args()
@@ -263,6 +265,123 @@ def run_batched(args, g, torch, stream, dev):
             "graphs": True}
 
 
+def run_serving(args, g, device):
+    """Serving: an open-loop Poisson stream of host-memory requests (sizes of
+    the mixed batch's texture levels plus a 1024x1024 probe class at 10% of
+    arrivals, BC1 / ETC1s 50/50, pinned inputs and outputs), offered at
+    10/25/50/75/90% of the server's measured capacity.  Capacity = the same
+    request mix all arriving at once.  Both data paths of the server are run;
+    the plain loop (one request per launch, sequential) is the baseline."""
+    import numpy as np
+
+    from goofy_gb300 import workloads
+
+    rng = np.random.default_rng(4)
+    specs = [(lv["width"], lv["height"]) for lv in workloads.texture_batch(1000, with_pixels=False)]
+    sizes = sorted(set(specs) | {(1024, 1024)})
+    pinned = []
+
+    def pin(nbytes):
+        arr, ptr = g.pinned_array(nbytes)
+        pinned.append(ptr)
+        return arr, ptr
+
+    src = {}
+    for (w, h) in sizes:
+        arr, ptr = pin(w * h * 4)
+        arr.reshape(h, 4 * w)[:] = workloads.scene(w, h, 7000 + w * 3 + h)
+        src[(w, h)] = ptr
+    ring_bytes = 1 << 29
+    _, out_ptr = pin(ring_bytes)
+
+    def stream(n, rate_per_s):
+        """n requests: sizes, codecs, arrival offsets (ns), output offsets in the ring."""
+        probe = rng.random(n) < 0.10
+        pick = rng.integers(0, len(specs), n)
+        wh = [(1024, 1024) if probe[i] else specs[pick[i]] for i in range(n)]
+        codec = rng.integers(0, 2, n)
+        if rate_per_s is None:
+            arrival = np.zeros(n, np.int64)
+        else:
+            arrival = np.cumsum(rng.exponential(1e9 / rate_per_s, n)).astype(np.int64)
+        reqs, off = [], 0
+        for i in range(n):
+            w, h = wh[i]
+            nb = (w // 4) * (h // 4) * 8
+            if off + nb > ring_bytes:
+                off = 0
+            reqs.append((src[(w, h)], out_ptr + off, w, h, 4 * w, int(codec[i])))
+            off += (nb + 255) // 256 * 256
+        return reqs, arrival, np.array([w * h for (w, h) in wh], np.int64), probe
+
+    def classes(px, probe, lat_ns):
+        out = {}
+        groups = {"probe_1024x1024": probe, "small_le_128x128": (~probe) & (px <= 128 * 128),
+                  "medium_le_512x512": (~probe) & (px > 128 * 128) & (px <= 512 * 512),
+                  "large_gt_512x512": (~probe) & (px > 512 * 512)}
+        for k, m in groups.items():
+            if m.any():
+                v = lat_ns[m] / 1e6
+                out[k] = {"n": int(m.sum()), "p50_ms": round(float(np.percentile(v, 50)), 3),
+                          "p99_ms": round(float(np.percentile(v, 99)), 3)}
+        return out
+
+    result = {"workload": "open-loop Poisson requests: sizes of the 1000-texture batch's levels + 10% 1024x1024 "
+                          "probe, BC1/ETC1s 50/50, pinned host in/out, device budget 16 GiB",
+              "offered_load_basis": "fraction of the server's own measured capacity (all requests arriving at "
+                                    "once); every request crosses the host link, whose measured H2D ceiling "
+                                    "(~211 GB/s) caps serving far below the device-resident batched rate"}
+    try:
+        for name, mode in (("staged", g.SERVER_STAGED), ("direct", g.SERVER_DIRECT)):
+            srv = g.Server(mode=mode, device=device)
+            try:
+                n_sat = 20000
+                reqs, arrival, px, probe = stream(n_sat, None)
+                rc, lat, wall = srv.replay(reqs, arrival)
+                assert rc == g.OK, g.last_error()
+                cap = float(px.sum()) / (wall / 1e9)
+                entry = {"capacity_mpix_s": round(cap / 1e6, 1), "capacity_requests": n_sat,
+                         "mean_request_px": round(float(px.mean()))}
+                loads = {}
+                for f in (0.10, 0.25, 0.50, 0.75, 0.90):
+                    rate = f * cap / float(px.mean())
+                    n = max(200, int(rate * args.serve_seconds))
+                    reqs, arrival, rpx, rprobe = stream(n, rate)
+                    rc, lat, wall = srv.replay(reqs, arrival)
+                    assert rc == g.OK, g.last_error()
+                    loads["%d%%" % round(100 * f)] = {
+                        "offered_mpix_s": round(f * cap / 1e6, 1), "requests": n,
+                        "sustained_mpix_s": round(float(rpx.sum()) / (wall / 1e9) / 1e6, 1),
+                        "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
+                        "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
+                        "by_class": classes(rpx, rprobe, lat)}
+                entry["loads"] = loads
+                entry["stats"] = srv.stats()
+                result[name] = entry
+            finally:
+                srv.close()
+        n_plain = 4000
+        reqs, arrival, px, probe = stream(n_plain, None)
+        rc, lat, wall = g.plain_replay(reqs, arrival, device)
+        assert rc == g.OK, g.last_error()
+        plain_cap = float(px.sum()) / (wall / 1e9)
+        best = max(result["staged"]["capacity_mpix_s"], result["direct"]["capacity_mpix_s"])
+        result["plain"] = {"capacity_mpix_s": round(plain_cap / 1e6, 1), "requests": n_plain,
+                           "server_vs_plain": round(best * 1e6 / plain_cap, 2)}
+        f = 0.5
+        rate = f * plain_cap / float(px.mean())
+        n = max(200, int(rate * args.serve_seconds))
+        reqs, arrival, rpx, rprobe = stream(n, rate)
+        rc, lat, wall = g.plain_replay(reqs, arrival, device)
+        result["plain"]["at_50pct_of_own_capacity"] = {
+            "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
+            "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3), "by_class": classes(rpx, rprobe, lat)}
+    finally:
+        for p in pinned:
+            g.host_free(p)
+    return result
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -455,6 +574,9 @@ def run_gpu(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(args, g, torch, stream, dev)
+    serving = None
+    if not args.no_serving:
+        serving = run_serving(args, g, local)
     if not args.no_cpu:
         from oracle import build as oracle_build
 
@@ -468,6 +590,7 @@ def run_gpu(args):
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
             "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+            "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
     print(json.dumps(line), flush=True)

@@ -45,6 +45,32 @@ _VP = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 
 
+SERVER_STAGED = 0
+SERVER_DIRECT = 1
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("mode", ctypes.c_int32), ("device_budget_bytes", ctypes.c_uint64),
+                ("max_batch_images", ctypes.c_uint32), ("max_inflight_batches", ctypes.c_uint32),
+                ("max_requests", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Request(ctypes.Structure):
+    """goofy_gpu_request: one host-memory encode request."""
+    _fields_ = [("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("stride", ctypes.c_uint32), ("codec", ctypes.c_int32)]
+
+
+class RequestTimes(ctypes.Structure):
+    _fields_ = [("submit_ns", ctypes.c_int64), ("admit_ns", ctypes.c_int64), ("launch_ns", ctypes.c_int64),
+                ("done_ns", ctypes.c_int64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_uint64), ("requests_done", ctypes.c_uint64), ("pixels_done", ctypes.c_uint64),
+                ("max_batch", ctypes.c_uint64), ("waiting", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64)]
+
+
 class Tile(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
                 ("persistent", ctypes.c_uint32)]
@@ -88,6 +114,16 @@ def _declare(lib):
         "goofy_gpu_batch_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Image), _U32, _U32, ctypes.POINTER(BatchTile),
                                                     ctypes.POINTER(ctypes.c_float)]),
         "goofy_gpu_batch_encode_noalloc": (ctypes.c_int, [ctypes.POINTER(Image), _U32, _VP]),
+        "goofy_gpu_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
+        "goofy_gpu_server_create": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.POINTER(ServerConfig)]),
+        "goofy_gpu_server_destroy": (None, [_VP]),
+        "goofy_gpu_server_submit": (ctypes.c_int, [_VP, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+        "goofy_gpu_server_wait": (ctypes.c_int, [_VP, ctypes.c_uint64, _U32, ctypes.POINTER(RequestTimes)]),
+        "goofy_gpu_server_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServerStats)]),
+        "goofy_gpu_now_ns": (ctypes.c_int64, []),
+        "goofy_gpu_server_replay": (ctypes.c_int, [_VP, ctypes.POINTER(Request), _VP, _U32, _VP, ctypes.POINTER(ctypes.c_int64)]),
+        "goofy_gpu_plain_replay": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Request), _VP, _U32, _VP,
+                                                  ctypes.POINTER(ctypes.c_int64)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -285,3 +321,91 @@ def batch_encode_noalloc(images, stream=None):
     the library; calls sharing it must not overlap on the GPU)."""
     arr = images if isinstance(images, ctypes.Array) else images_array(images)
     return lib().goofy_gpu_batch_encode_noalloc(arr, len(arr), stream)
+
+
+def requests_array(reqs):
+    """ctypes array of Request from (src, dst, width, height, stride, codec) tuples."""
+    arr = (Request * len(reqs))()
+    for i, q in enumerate(reqs):
+        arr[i] = q if isinstance(q, Request) else Request(_addr(q[0]), _addr(q[1]), *q[2:])
+    return arr
+
+
+class Server:
+    """goofy_gpu_server: continuous-batching server for host-memory requests."""
+
+    def __init__(self, mode=SERVER_STAGED, device_budget_bytes=16 << 30, max_batch_images=1024,
+                 max_inflight_batches=4, max_requests=1 << 20, device=0):
+        cfg = ServerConfig()
+        lib().goofy_gpu_server_default_config(ctypes.byref(cfg))
+        cfg.device, cfg.mode, cfg.device_budget_bytes = device, mode, device_budget_bytes
+        cfg.max_batch_images, cfg.max_inflight_batches, cfg.max_requests = (max_batch_images, max_inflight_batches,
+                                                                            max_requests)
+        h = ctypes.c_void_p()
+        rc = lib().goofy_gpu_server_create(ctypes.byref(h), ctypes.byref(cfg))
+        if rc != OK:
+            raise RuntimeError("goofy_gpu_server_create: %s %s" % (status_string(rc), last_error()))
+        self._h = h
+
+    def submit(self, codec, dst, src, width, height, stride):
+        """Returns (status, ticket)."""
+        t = ctypes.c_uint64()
+        q = Request(_addr(src), _addr(dst), width, height, stride, codec)
+        rc = lib().goofy_gpu_server_submit(self._h, ctypes.byref(q), ctypes.byref(t))
+        return rc, t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        """Returns (status, RequestTimes)."""
+        tm = RequestTimes()
+        rc = lib().goofy_gpu_server_wait(self._h, ticket, timeout_ms, ctypes.byref(tm))
+        return rc, tm
+
+    def stats(self):
+        st = ServerStats()
+        assert lib().goofy_gpu_server_get_stats(self._h, ctypes.byref(st)) == OK
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def replay(self, reqs, arrival_ns):
+        """Open-loop replay; returns (status, latency_ns int64 array, wall_ns)."""
+        import numpy as np
+
+        arr = reqs if isinstance(reqs, ctypes.Array) else requests_array(reqs)
+        arrival = np.ascontiguousarray(arrival_ns, dtype=np.int64)
+        lat = np.zeros(len(arr), np.int64)
+        wall = ctypes.c_int64()
+        rc = lib().goofy_gpu_server_replay(self._h, arr, arrival.ctypes.data, len(arr), lat.ctypes.data,
+                                           ctypes.byref(wall))
+        return rc, lat, wall.value
+
+    def close(self):
+        if self._h:
+            lib().goofy_gpu_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plain_replay(reqs, arrival_ns, device=0):
+    """The plain loop (one request per launch, sequential); (status, latency_ns, wall_ns)."""
+    import numpy as np
+
+    arr = reqs if isinstance(reqs, ctypes.Array) else requests_array(reqs)
+    arrival = np.ascontiguousarray(arrival_ns, dtype=np.int64)
+    lat = np.zeros(len(arr), np.int64)
+    wall = ctypes.c_int64()
+    rc = lib().goofy_gpu_plain_replay(device, arr, arrival.ctypes.data, len(arr), lat.ctypes.data, ctypes.byref(wall))
+    return rc, lat, wall.value
+
+
+def pinned_array(nbytes):
+    """numpy uint8 view of a fresh pinned host buffer (freed with free_pinned)."""
+    import numpy as np
+
+    p = host_alloc(nbytes)
+    if not p:
+        raise MemoryError("pinned allocation of %d bytes failed" % nbytes)
+    return np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p)), p

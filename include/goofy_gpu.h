@@ -152,6 +152,80 @@ int goofy_gpu_batch_set_tile(goofy_gpu_batch* batch, const goofy_gpu_batch_tile*
 int goofy_gpu_batch_autotune(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, uint32_t reps,
                              goofy_gpu_batch_tile* best, float* best_us);
 
+/* ---- serving: continuous batching of host-memory requests ----------------- */
+
+#define GOOFY_SERVER_STAGED 0 /* requests copied into a device arena, encoded there, copied back */
+#define GOOFY_SERVER_DIRECT 1 /* the batch kernel reads / writes the requests' host buffers itself */
+
+typedef struct goofy_gpu_server goofy_gpu_server;
+
+typedef struct goofy_gpu_server_config {
+    int32_t device;
+    int32_t mode;                  /* GOOFY_SERVER_STAGED or GOOFY_SERVER_DIRECT */
+    uint64_t device_budget_bytes;  /* admission budget: arena size (staged) or bytes in flight (direct) */
+    uint32_t max_batch_images;     /* requests folded into one launch */
+    uint32_t max_inflight_batches; /* launches on the GPU at once */
+    uint32_t max_requests;         /* unreleased tickets at once */
+    uint32_t reserved;
+} goofy_gpu_server_config;
+
+/* One encode request on host memory (pinned buffers are copied by DMA / read
+ * by the GPU directly; direct mode needs GPU-accessible buffers). */
+typedef struct goofy_gpu_request {
+    const uint8_t* src;
+    uint8_t* dst;
+    uint32_t width, height, stride;
+    int32_t codec;
+} goofy_gpu_request;
+
+typedef struct goofy_gpu_request_times {
+    int64_t submit_ns, admit_ns, launch_ns, done_ns; /* goofy_gpu_now_ns() clock */
+} goofy_gpu_request_times;
+
+typedef struct goofy_gpu_server_stats {
+    uint64_t launches, requests_done, pixels_done, max_batch, waiting, inflight_bytes;
+} goofy_gpu_server_stats;
+
+/* Defaults: device 0, staged, 16 GiB budget, 1024 requests per launch, 4
+ * launches in flight, 2^20 tickets.  No reference counterpart (the reference
+ * is a synchronous per-image function). */
+void goofy_gpu_server_default_config(goofy_gpu_server_config* cfg);
+
+/* Start a server (allocates its arena, launch slots and streams once, and a
+ * scheduler thread).  Requests that arrive while others run are admitted as
+ * budget frees up and join the next launch of the persistent batch kernel. */
+int goofy_gpu_server_create(goofy_gpu_server** server, const goofy_gpu_server_config* cfg);
+
+/* Stop after finishing everything submitted; release all resources. */
+void goofy_gpu_server_destroy(goofy_gpu_server* server);
+
+/* Queue one request; never blocks on the GPU.  GOOFY_ERR_TOO_LARGE if the
+ * request alone exceeds the budget, GOOFY_ERR_BUSY if max_requests tickets
+ * are unreleased.  Output equals goofy_gpu_compress_host on the same request. */
+int goofy_gpu_server_submit(goofy_gpu_server* server, const goofy_gpu_request* req, uint64_t* ticket);
+
+/* Wait up to timeout_ms for a ticket; on completion returns its status, fills
+ * `times` (may be NULL) and releases the ticket.  GOOFY_ERR_TIMEOUT leaves the
+ * ticket pending. */
+int goofy_gpu_server_wait(goofy_gpu_server* server, uint64_t ticket, uint32_t timeout_ms,
+                          goofy_gpu_request_times* times);
+
+int goofy_gpu_server_get_stats(goofy_gpu_server* server, goofy_gpu_server_stats* stats);
+
+/* Monotonic clock of the request timestamps, in nanoseconds. */
+int64_t goofy_gpu_now_ns(void);
+
+/* Open-loop load replay: submits reqs[i] at start + arrival_ns[i] while a
+ * second thread waits on the tickets; latency_ns[i] = completion - scheduled
+ * arrival (-1 if it failed); wall_ns = start to last completion. */
+int goofy_gpu_server_replay(goofy_gpu_server* server, const goofy_gpu_request* reqs, const int64_t* arrival_ns,
+                            uint32_t n, int64_t* latency_ns, int64_t* wall_ns);
+
+/* The same replay through the plain loop: one request at a time, each a
+ * host->device copy, one image-kernel launch and a device->host copy. */
+int goofy_gpu_plain_replay(int device, const goofy_gpu_request* reqs, const int64_t* arrival_ns, uint32_t n,
+                           int64_t* latency_ns, int64_t* wall_ns);
+
 /* ---- batch encoding without any allocation ---------------------------------- */
 
 /* Largest image count goofy_gpu_batch_encode_noalloc takes per call. */
