@@ -45,6 +45,10 @@ _VP = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 
 
+HOST_PATH_AUTO = 0
+HOST_PATH_STAGED = 1
+HOST_PATH_DIRECT = 2
+
 SERVER_STAGED = 0
 SERVER_DIRECT = 1
 
@@ -100,6 +104,8 @@ def _declare(lib):
         "goofy_gpu_compress_bc1_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
         "goofy_gpu_compress_etc1s_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
         "goofy_gpu_host_alloc": (_VP, [ctypes.c_size_t]),
+        "goofy_gpu_set_host_path": (ctypes.c_int, [ctypes.c_int]),
+        "goofy_gpu_get_host_path": (ctypes.c_int, []),
         "goofy_gpu_host_free": (None, [_VP]),
         "goofy_gpu_get_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
         "goofy_gpu_set_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
@@ -220,6 +226,14 @@ def init(device=0):
 
 def shutdown():
     lib().goofy_gpu_shutdown()
+
+
+def set_host_path(path):
+    return lib().goofy_gpu_set_host_path(path)
+
+
+def get_host_path():
+    return lib().goofy_gpu_get_host_path()
 
 
 def host_alloc(nbytes):

@@ -50,7 +50,7 @@ struct goofy_gpu_batch {
     std::mutex mu;
     int device = 0;
     uint32_t max_images = 0;
-    BatchTile tile{256, 2, 256};
+    BatchTile tile{128, 1, 256};
     bool graphs = true;
     cudaStream_t stream = nullptr;
     cudaEvent_t caller_ready = nullptr;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -72,6 +73,7 @@ struct Buffer {
 struct HostPath {
     std::mutex mu;
     bool ready = false;
+    bool pageable_ok = false;  // kernels may read / write pageable host memory
     int device = 0;
     cudaStream_t stream[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr};
@@ -109,6 +111,10 @@ struct HostPath {
         DeviceGuard g(dev);
         CUDA_TRY(g.err);
         device = dev;
+        int pageable = 0, ats = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+        pageable_ok = pageable && ats;
         for (int i = 0; i < 2; ++i) {
             CUDA_TRY(cudaStreamCreateWithFlags(&stream[i], cudaStreamNonBlocking));
             CUDA_TRY(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
@@ -153,6 +159,27 @@ bool is_pinned(const void* p)
     return a.type == cudaMemoryTypeHost;
 }
 
+std::atomic<int> g_host_path{GOOFY_HOST_PATH_AUTO};
+
+// Address under which the current device's kernels can use host buffer `p`
+// directly, or nullptr: pinned memory (its mapped address), device or managed
+// memory, or -- where the GPU walks the host page tables (NVLink-C2C
+// address translation) -- ordinary pageable memory.
+const void* device_view(const void* p, bool pageable_ok)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    switch (a.type) {
+    case cudaMemoryTypeHost: return a.devicePointer;
+    case cudaMemoryTypeDevice:
+    case cudaMemoryTypeManaged: return p;
+    default: return pageable_ok ? p : nullptr;
+    }
+}
+
 int check_args(int codec, const void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride)
 {
     if (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S) return GOOFY_ERR_INVALID;
@@ -178,6 +205,26 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
     }
     DeviceGuard g(hp.device);
     CUDA_TRY(g.err);
+
+    // Direct path: one kernel reads the caller's rows and writes its blocks
+    // over the host link, no staging copies.
+    const int path = g_host_path.load();
+    if (path != GOOFY_HOST_PATH_STAGED) {
+        const void* dsrc = device_view(src, hp.pageable_ok);
+        void* ddst = const_cast<void*>(device_view(dst, hp.pageable_ok));
+        const uintptr_t sa = reinterpret_cast<uintptr_t>(dsrc);
+        const bool aligned = sa % 4 == 0 && stride % 4 == 0 && reinterpret_cast<uintptr_t>(ddst) % 8 == 0;
+        if (dsrc && ddst && aligned) {
+            const SrcAccess access = (sa % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
+            CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(dsrc), stride,
+                                             static_cast<uint8_t*>(ddst), width, height, tile_for(codec), access,
+                                             hp.stream[0]));
+            CUDA_TRY(cudaStreamSynchronize(hp.stream[0]));
+            return GOOFY_OK;
+        }
+        if (path == GOOFY_HOST_PATH_DIRECT)
+            return goofy_gpu::fail(GOOFY_ERR_INVALID, "direct host path: buffers not GPU-accessible or misaligned");
+    }
 
     const uint32_t bw = width / 4, bh = height / 4;
     const size_t row_bytes = 4ull * width;
@@ -320,6 +367,16 @@ GOOFY_EXPORT int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src,
 {
     return compress_host_impl(GOOFY_CODEC_ETC1S, dst, src, width, height, stride);
 }
+
+GOOFY_EXPORT int goofy_gpu_set_host_path(int path)
+{
+    if (path != GOOFY_HOST_PATH_AUTO && path != GOOFY_HOST_PATH_STAGED && path != GOOFY_HOST_PATH_DIRECT)
+        return GOOFY_ERR_INVALID;
+    g_host_path.store(path);
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_get_host_path(void) { return g_host_path.load(); }
 
 GOOFY_EXPORT void* goofy_gpu_host_alloc(size_t bytes)
 {

@@ -86,6 +86,19 @@ int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src, uint32_t wid
 int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                             uint32_t stride);
 
+/* How the host-pointer entry points move data (process-wide setting):
+ * AUTO (default): DIRECT when both buffers are GPU-accessible -- pinned
+ * memory, or any host memory where the GPU walks the host page tables
+ * (Grace-Blackwell NVLink-C2C) -- and suitably aligned, else STAGED.
+ * STAGED: copy bands into device buffers, encode there, copy back.
+ * DIRECT: one kernel reads the caller's rows and writes its blocks over the
+ * host link; GOOFY_ERR_INVALID if the buffers do not allow it. */
+#define GOOFY_HOST_PATH_AUTO 0
+#define GOOFY_HOST_PATH_STAGED 1
+#define GOOFY_HOST_PATH_DIRECT 2
+int goofy_gpu_set_host_path(int path);
+int goofy_gpu_get_host_path(void);
+
 /* ---- pinned host memory (for callers that want the fast host path) -------- */
 void* goofy_gpu_host_alloc(size_t bytes);
 void goofy_gpu_host_free(void* p);

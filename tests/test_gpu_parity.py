@@ -81,9 +81,19 @@ def test_strides_and_alignment(cuda, name, codec, extra, offset):
 
 
 @pytest.mark.parametrize("name,codec", CODECS)
-def test_host_path_pinned_and_pageable(cuda, name, codec):
-    """goofy_gpu_compress_host / goofy::compress*: multi-band pipeline (64 MiB
-    image), pageable and pinned buffers, padded stride."""
+@pytest.mark.parametrize("path", [g.HOST_PATH_AUTO, g.HOST_PATH_STAGED, g.HOST_PATH_DIRECT])
+def test_host_path_pinned_and_pageable(cuda, name, codec, path):
+    """goofy_gpu_compress_host / goofy::compress*: 64 MiB image through the
+    staged band pipeline or the direct path, pageable and pinned buffers,
+    padded stride."""
+    assert g.set_host_path(path) == g.OK
+    try:
+        _host_path_case(codec)
+    finally:
+        g.set_host_path(g.HOST_PATH_AUTO)
+
+
+def _host_path_case(codec):
     w, h = 4096, 4096
     stride = 4 * w + 64
     img = np.zeros((h, stride), np.uint8)
