@@ -594,6 +594,26 @@ def run_gpu(args):
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s"}
     cpu = None
+    # quality: RGB PSNR of the timed outputs (the reference harness's secondary
+    # metric), and the speed of the fused decode + squared-error kernel
+    quality = {}
+    d_sums = torch.zeros(5, dtype=torch.int64, device=dev)
+    for c in codecs:
+        rc, psnr, sums = g.psnr_rgb(c, dst[c], src[c], W, H, 4 * W)
+        assert rc == g.OK, g.last_error()
+        ts = []
+        for r in range(8):
+            d_sums.zero_()
+            e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e_a.record(stream)
+            g.block_error_device(c, dst[c], src[(c + 1) % 2], W, H, 4 * W, d_sums, sh)
+            e_b.record(stream)
+            e_b.synchronize()
+            ts.append(e_a.elapsed_time(e_b))
+        ms = statistics.median(ts[2:])
+        quality[names[c]] = {"psnr_rgb_db": round(psnr, 5), "unsupported_blocks": int(sums[4]),
+                             "decode_error_kernel_us": round(ms * 1e3, 2),
+                             "decode_error_hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
     batched = None
     if not args.no_batched:
         batched = run_batched(args, g, torch, stream, dev)
@@ -612,7 +632,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}

@@ -120,6 +120,10 @@ def _declare(lib):
         "goofy_gpu_batch_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Image), _U32, _U32, ctypes.POINTER(BatchTile),
                                                     ctypes.POINTER(ctypes.c_float)]),
         "goofy_gpu_batch_encode_noalloc": (ctypes.c_int, [ctypes.POINTER(Image), _U32, _VP]),
+        "goofy_gpu_decode_device": (ctypes.c_int, [ctypes.c_int, _VP, _U32, _VP, _U32, _U32, _VP, _VP]),
+        "goofy_gpu_block_error_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
+        "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
+                                              ctypes.POINTER(ctypes.c_double), _VP]),
         "goofy_gpu_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
         "goofy_gpu_server_create": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.POINTER(ServerConfig)]),
         "goofy_gpu_server_destroy": (None, [_VP]),
@@ -423,3 +427,25 @@ def pinned_array(nbytes):
     if not p:
         raise MemoryError("pinned allocation of %d bytes failed" % nbytes)
     return np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p)), p
+
+
+def decode_device(codec, rgba, rgba_stride, blocks, width, height, d_unsupported, stream=None):
+    """GPU decode of device blocks into device RGBA8 rows (see goofy_gpu_decode_device)."""
+    return lib().goofy_gpu_decode_device(codec, _addr(rgba), rgba_stride, _addr(blocks), width, height,
+                                         _addr(d_unsupported), stream)
+
+
+def block_error_device(codec, blocks, src, width, height, stride, d_sums, stream=None):
+    return lib().goofy_gpu_block_error_device(codec, _addr(blocks), _addr(src), width, height, stride,
+                                              _addr(d_sums), stream)
+
+
+def psnr_rgb(codec, blocks, src, width, height, stride):
+    """(status, RGB PSNR as the reference reports it, [sumR, sumG, sumB, sumA, unsupported])."""
+    import numpy as np
+
+    out = ctypes.c_double()
+    sums = np.zeros(5, np.uint64)
+    rc = lib().goofy_gpu_psnr_rgb(codec, _addr(blocks), _addr(src), width, height, stride, ctypes.byref(out),
+                                  sums.ctypes.data)
+    return rc, out.value, sums

@@ -1,0 +1,235 @@
+// decode_kernels.cu -- BC1 / ETC1 block decoding and the encode-quality error
+// reduction on sm_103a.
+//
+// The reference checks quality on the CPU: it decodes every block with its
+// harness decoders (Src/decoder.cpp: DecompressColour :819-871 for BC1,
+// decompressBlockDiffFlipC :388-678 for ETC1) and sums squared channel
+// differences in getMsePsnr (Src/main.cpp:403-469).  Here one thread decodes
+// one block (BC1: both endpoint orders; ETC1: individual and differential
+// modes, both flips; ETC2-only differential overflows are counted as
+// unsupported and decoded as black) and either stores the 16 pixels or
+// compares them with the source pixels, summing squared differences per
+// channel exactly in integers (warp shuffles, then one 64-bit atomic per warp
+// and channel).
+#include <cuda_runtime.h>
+
+#include "block_codec.cuh"
+#include "decode.h"
+#include "device_io.cuh"
+
+namespace goofy_gpu {
+
+// 5/6-bit endpoint channel to 8 bits: (c << 3) | (c >> 2), (c << 2) | (c >> 4).
+__device__ __forceinline__ uint32_t expand565(uint32_t v)
+{
+    const uint32_t r = (v >> 11) & 31u, g = (v >> 5) & 63u, b = v & 31u;
+    return (r << 3 | r >> 2) | (g << 2 | g >> 4) << 8 | (b << 3 | b >> 2) << 16 | 0xff000000u;
+}
+
+__device__ __forceinline__ uint32_t chan(uint32_t w, int c) { return (w >> (8 * c)) & 0xffu; }
+
+// Palette of a BC1 block as four RGBA words.
+__device__ __forceinline__ void bc1_palette(uint32_t ends, uint32_t (&pal)[4])
+{
+    const uint32_t a = ends & 0xffffu, b = ends >> 16;
+    pal[0] = expand565(a);
+    pal[1] = expand565(b);
+    uint32_t p2 = 0, p3 = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const uint32_t p = chan(pal[0], c), q = chan(pal[1], c);
+        if (a > b) {
+            p2 |= ((2 * p + q) / 3) << (8 * c);
+            p3 |= ((p + 2 * q) / 3) << (8 * c);
+        } else {
+            p2 |= ((p + q) / 2) << (8 * c);
+        }
+    }
+    pal[2] = p2 | 0xff000000u;
+    pal[3] = a > b ? (p3 | 0xff000000u) : 0u;  // 3-colour mode: transparent black
+}
+
+// The 4 colours of one ETC1 sub-block: clamp(base + modifier) per channel.
+__device__ __forceinline__ void etc1_subpalette(uint32_t base, uint32_t table, uint32_t (&pal)[4])
+{
+    const int small = table == 0 ? 2 : table == 1 ? 5 : table == 2 ? 9 : table == 3 ? 13
+                    : table == 4 ? 18 : table == 5 ? 24 : table == 6 ? 33 : 47;
+    const int large = table == 0 ? 8 : table == 1 ? 17 : table == 2 ? 29 : table == 3 ? 42
+                    : table == 4 ? 60 : table == 5 ? 80 : table == 6 ? 106 : 183;
+    const int mod[4] = {small, large, -small, -large};  // pixel index value 0..3
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint32_t w = 0xff000000u;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int v = (int)chan(base, c) + mod[k];
+            w |= (uint32_t)min(max(v, 0), 255) << (8 * c);
+        }
+        pal[k] = w;
+    }
+}
+
+// Decode one block into 16 row-major RGBA words.  Returns false for an ETC1
+// differential block whose second colour leaves 0..31 (an ETC2 mode).
+template <int CODEC>
+__device__ __forceinline__ bool decode_block(uint2 blk, uint32_t (&px)[16])
+{
+    if constexpr (CODEC == kBC1) {
+        uint32_t pal[4];
+        bc1_palette(blk.x, pal);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t idx = (blk.y >> (2 * i)) & 3u;
+            px[i] = idx == 0 ? pal[0] : idx == 1 ? pal[1] : idx == 2 ? pal[2] : pal[3];
+        }
+        return true;
+    } else {
+        // the block is big-endian: bytes 0..3 of blk.x are bits 63..32
+        const uint32_t w0 = __byte_perm(blk.x, 0, 0x0123), w1 = __byte_perm(blk.y, 0, 0x0123);
+        const bool diff = (w0 >> 1) & 1u, flip = w0 & 1u;
+        uint32_t base[2] = {0, 0};
+        bool ok = true;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            uint32_t b0, b1;
+            if (diff) {
+                const int c5 = (int)(w0 >> (27 - 8 * c)) & 31;
+                int d = (int)(w0 >> (24 - 8 * c)) & 7;
+                d = d >= 4 ? d - 8 : d;
+                const int c52 = c5 + d;
+                ok = ok && c52 >= 0 && c52 <= 31;
+                const int c5b = min(max(c52, 0), 31);
+                b0 = (uint32_t)(c5 << 3 | c5 >> 2);
+                b1 = (uint32_t)(c5b << 3 | c5b >> 2);
+            } else {
+                const uint32_t a = (w0 >> (28 - 8 * c)) & 15u, b = (w0 >> (24 - 8 * c)) & 15u;
+                b0 = a << 4 | a;
+                b1 = b << 4 | b;
+            }
+            base[0] |= b0 << (8 * c);
+            base[1] |= b1 << (8 * c);
+        }
+        uint32_t pal0[4], pal1[4];
+        etc1_subpalette(base[0], (w0 >> 5) & 7u, pal0);
+        etc1_subpalette(base[1], (w0 >> 2) & 7u, pal1);
+#pragma unroll
+        for (int y = 0; y < 4; ++y)
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                const int k = 4 * x + y;
+                const uint32_t idx = ((w1 >> (16 + k)) & 1u) << 1 | ((w1 >> k) & 1u);
+                const bool sub = flip ? (y >= 2) : (x >= 2);
+                const uint32_t a = idx == 0 ? pal0[0] : idx == 1 ? pal0[1] : idx == 2 ? pal0[2] : pal0[3];
+                const uint32_t b = idx == 0 ? pal1[0] : idx == 1 ? pal1[1] : idx == 2 ? pal1[2] : pal1[3];
+                px[4 * y + x] = ok ? (sub ? b : a) : 0u;
+            }
+        return ok;
+    }
+}
+
+__device__ __forceinline__ uint2 load_block8(const uint8_t* p)
+{
+    uint2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+template <int CODEC>
+__global__ void __launch_bounds__(256) decode_image_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
+                                                           uint32_t nblk, uint8_t* __restrict__ rgba, size_t stride,
+                                                           unsigned long long* __restrict__ unsupported)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = true;
+    if (i < nblk) {
+        const uint32_t by = i / bw, bx = i - by * bw;
+        uint32_t px[16];
+        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
+        uint8_t* row = rgba + (size_t)by * 4u * stride + 16u * (size_t)bx;
+#pragma unroll
+        for (int y = 0; y < 4; ++y)
+            *reinterpret_cast<uint4*>(row + (size_t)y * stride) = make_uint4(px[4 * y], px[4 * y + 1], px[4 * y + 2],
+                                                                             px[4 * y + 3]);
+    }
+    const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+    if (bad && (threadIdx.x & 31u) == 0) atomicAdd(unsupported, (unsigned long long)__popc(bad));
+}
+
+// Sums of squared channel differences of one 4-pixel row: |a-b| per byte,
+// bytes regrouped so each word holds one channel of the 4 pixels, then a
+// dot product of each channel word with itself.
+__device__ __forceinline__ void accumulate_row(const uint32_t (&a)[4], const uint32_t (&b)[4], uint32_t (&acc)[4])
+{
+    uint32_t d[4];
+#pragma unroll
+    for (int x = 0; x < 4; ++x) d[x] = __vabsdiffu4(a[x], b[x]);
+    const uint32_t t0 = __byte_perm(d[0], d[1], 0x5140), t1 = __byte_perm(d[2], d[3], 0x5140);
+    const uint32_t t2 = __byte_perm(d[0], d[1], 0x7362), t3 = __byte_perm(d[2], d[3], 0x7362);
+    const uint32_t ch[4] = {__byte_perm(t0, t1, 0x5410), __byte_perm(t0, t1, 0x7632), __byte_perm(t2, t3, 0x5410),
+                            __byte_perm(t2, t3, 0x7632)};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[c] = __dp4a(ch[c], ch[c], acc[c]);
+}
+
+template <int CODEC>
+__global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
+                                                          uint32_t nblk, const uint8_t* __restrict__ src,
+                                                          size_t stride, bool vec16,
+                                                          unsigned long long* __restrict__ sums)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
+    bool ok = true;
+    if (i < nblk) {
+        const uint32_t by = i / bw, bx = i - by * bw;
+        uint32_t px[16], w[16];
+        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
+        load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+            const uint32_t a[4] = {w[4 * y], w[4 * y + 1], w[4 * y + 2], w[4 * y + 3]};
+            const uint32_t b[4] = {px[4 * y], px[4 * y + 1], px[4 * y + 2], px[4 * y + 3]};
+            accumulate_row(a, b, acc);
+        }
+    }
+    unsigned long long s[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        s[c] = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+    }
+    const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+    if ((threadIdx.x & 31u) == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (s[c]) atomicAdd(&sums[c], s[c]);
+        if (bad) atomicAdd(&sums[4], (unsigned long long)__popc(bad));
+    }
+}
+
+cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint32_t height, uint8_t* rgba,
+                          size_t stride, unsigned long long* unsupported, cudaStream_t stream)
+{
+    const uint32_t bw = width / 4, nblk = bw * (height / 4);
+    if (nblk == 0) return cudaSuccess;
+    const uint32_t grid = (nblk + 255) / 256;
+    if (codec == kBC1) decode_image_kernel<kBC1><<<grid, 256, 0, stream>>>(blocks, bw, nblk, rgba, stride, unsupported);
+    else decode_image_kernel<kETC1S><<<grid, 256, 0, stream>>>(blocks, bw, nblk, rgba, stride, unsupported);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* src, uint32_t width, uint32_t height,
+                               size_t stride, bool vec16, unsigned long long* sums, cudaStream_t stream)
+{
+    const uint32_t bw = width / 4, nblk = bw * (height / 4);
+    if (nblk == 0) return cudaSuccess;
+    const uint32_t grid = (nblk + 255) / 256;
+    if (codec == kBC1)
+        block_error_kernel<kBC1><<<grid, 256, 0, stream>>>(blocks, bw, nblk, src, stride, vec16, sums);
+    else
+        block_error_kernel<kETC1S><<<grid, 256, 0, stream>>>(blocks, bw, nblk, src, stride, vec16, sums);
+    return cudaGetLastError();
+}
+
+}  // namespace goofy_gpu

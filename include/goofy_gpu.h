@@ -122,6 +122,30 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
 
+/* ---- decoding and encode quality -------------------------------------------- */
+
+/* Decode (width/4)*(height/4) blocks (device) into RGBA8 rows (device,
+ * `rgba` and `rgba_stride` 16-byte aligned), as the reference harness's
+ * decoders do (Src/decoder.cpp:933-971): BC1 in both endpoint orders; ETC1
+ * individual and differential modes with flip, alpha 255.  ETC1 differential
+ * blocks whose second colour leaves 0..31 (ETC2 modes) decode to zeros and
+ * are added to *d_unsupported (device uint64).  Asynchronous. */
+int goofy_gpu_decode_device(int codec, void* rgba, uint32_t rgba_stride, const void* blocks, uint32_t width,
+                            uint32_t height, uint64_t* d_unsupported, void* stream);
+
+/* Adds to d_sums[0..3] (device uint64) the per-channel sums of squared
+ * differences between `src` (RGBA8, 4-byte aligned rows) and its decoded
+ * `blocks`, and to d_sums[4] the unsupported-block count: the integer core
+ * of the reference's getMsePsnr (Src/main.cpp:403-469).  Asynchronous. */
+int goofy_gpu_block_error_device(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
+                                 uint32_t stride, uint64_t* d_sums, void* stream);
+
+/* Synchronous convenience: RGB PSNR (peak 768, as the reference reports it)
+ * of `blocks` against `src`, both on the current device; sums_out (may be
+ * NULL) receives the five accumulators. */
+int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
+                       uint32_t stride, double* psnr_rgb, uint64_t* sums_out);
+
 /* ---- batches: many device images of uneven sizes in one launch ----------- */
 
 /* One image of a batch (a texture or one of its mip levels).  src / dst and

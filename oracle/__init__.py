@@ -32,6 +32,14 @@ def load():
             fn.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U]
         lib.oracle_compress_mt.restype = ctypes.c_int
         lib.oracle_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
+        lib.oracle_decode_block.restype = ctypes.c_int
+        lib.oracle_decode_block.argtypes = [ctypes.c_int, _VP, _VP]
+        lib.oracle_decode_image.restype = ctypes.c_long
+        lib.oracle_decode_image.argtypes = [ctypes.c_int, _VP, _U, _U, _VP, _U]
+        lib.oracle_sq_error.restype = None
+        lib.oracle_sq_error.argtypes = [_VP, _U, _VP, _U, _U, _U, _VP]
+        lib.oracle_psnr_rgb.restype = ctypes.c_double
+        lib.oracle_psnr_rgb.argtypes = [_VP, _U, _U]
         _oracle = lib
     return _oracle
 
@@ -45,6 +53,8 @@ def load_ref():
         lib.ref_compress.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U]
         lib.ref_compress_mt.restype = ctypes.c_int
         lib.ref_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
+        lib.ref_decode_block.restype = None
+        lib.ref_decode_block.argtypes = [ctypes.c_int, _VP, _VP]
         _ref = lib
     return _ref
 
@@ -66,3 +76,29 @@ def encode(codec, img, width, height, stride=None, threads=1, any_width=True):
     if rc != 0:
         raise ValueError("oracle rejected the image: %d" % rc)
     return out
+
+
+def decode(codec, blocks, width, height):
+    """Oracle decode of (width/4)*(height/4) blocks into an RGBA8 image."""
+    import numpy as np
+
+    img = np.zeros((height, 4 * width), np.uint8)
+    bad = load().oracle_decode_image(codec, np.ascontiguousarray(blocks).ctypes.data, width, height, img.ctypes.data,
+                                     4 * width)
+    return img, bad
+
+
+def sq_error(a, b, width, height):
+    """Per-channel sums of squared differences (uint64[4]) of two RGBA8 images."""
+    import numpy as np
+
+    sums = np.zeros(4, np.uint64)
+    load().oracle_sq_error(a.ctypes.data, a.strides[0], b.ctypes.data, b.strides[0], width, height, sums.ctypes.data)
+    return sums
+
+
+def psnr_rgb(sums, width, height):
+    import numpy as np
+
+    s = np.ascontiguousarray(sums, dtype=np.uint64)
+    return load().oracle_psnr_rgb(s.ctypes.data, width, height)

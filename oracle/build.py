@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 REFERENCE_HEADER_DIR = "/root/reference/GoofyTC"
+REFERENCE_SRC_DIR = "/root/reference/Src"
 
 ORACLE_SO = os.path.join(BUILD_DIR, "libgoofy_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libgoofy_ref.so")
@@ -33,7 +34,7 @@ def oracle_cmd():
     src = os.path.join(HERE, "goofy_oracle.c")
     return [src, os.path.join(HERE, "goofy_oracle.h")], [
         "gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-        "-Wall", "-o", ORACLE_SO, src]
+        "-Wall", "-o", ORACLE_SO, src, "-lm"]
 
 
 def ref_available():
@@ -42,11 +43,14 @@ def ref_available():
 
 
 def ref_cmd():
+    """The reference encoder header and the reference harness's decoder
+    (Src/decoder.cpp, compiled from where it lies) behind ref_shim.cpp."""
     src = os.path.join(HERE, "ref_shim.cpp")
     hdr = os.path.join(REFERENCE_HEADER_DIR, "goofy_tc.h")
-    return [src, hdr], [
+    dec = os.path.join(REFERENCE_SRC_DIR, "decoder.cpp")
+    return [src, hdr, dec], [
         "g++", "-O3", "-DNDEBUG", "-std=c++17", "-fPIC", "-shared", "-pthread", "-msse2",
-        "-I", REFERENCE_HEADER_DIR, "-o", REF_SO, src]
+        "-I", REFERENCE_HEADER_DIR, "-I", REFERENCE_SRC_DIR, "-o", REF_SO, src, dec]
 
 
 def build(verbose=False):

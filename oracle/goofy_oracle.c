@@ -15,6 +15,8 @@
  */
 #include "goofy_oracle.h"
 
+#include <float.h>
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -200,4 +202,130 @@ int oracle_compress_mt(int codec, uint8_t* result, const uint8_t* input,
     free(job);
     free(started);
     return threads;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Decoding (test infrastructure: the quality check of the reference harness) */
+
+static void expand565(uint32_t v, uint8_t c[4])
+{
+    const uint32_t r = (v >> 11) & 31, g = (v >> 5) & 63, b = v & 31; /* Unpack565, decoder.cpp:799-816 */
+    c[0] = (uint8_t)(r << 3 | r >> 2);
+    c[1] = (uint8_t)(g << 2 | g >> 4);
+    c[2] = (uint8_t)(b << 3 | b >> 2);
+    c[3] = 255;
+}
+
+static void decode_bc1(const uint8_t blk[8], uint8_t out[64])
+{
+    uint8_t pal[4][4];
+    const uint32_t a = blk[0] | (uint32_t)blk[1] << 8, b = blk[2] | (uint32_t)blk[3] << 8;
+    expand565(a, pal[0]);
+    expand565(b, pal[1]);
+    for (int c = 0; c < 3; ++c) { /* decoder.cpp:828-843 */
+        const int p = pal[0][c], q = pal[1][c];
+        if (a <= b) {
+            pal[2][c] = (uint8_t)((p + q) / 2);
+            pal[3][c] = 0;
+        } else {
+            pal[2][c] = (uint8_t)((2 * p + q) / 3);
+            pal[3][c] = (uint8_t)((p + 2 * q) / 3);
+        }
+    }
+    pal[2][3] = 255;
+    pal[3][3] = a <= b ? 0 : 255;
+    for (int i = 0; i < 16; ++i) { /* row y in byte 4+y, pixel x at bits 2x, decoder.cpp:849-868 */
+        const int idx = (blk[4 + i / 4] >> (2 * (i % 4))) & 3;
+        memcpy(out + 4 * i, pal[idx], 4);
+    }
+}
+
+static const int etc1_modifiers[8][2] = {{2, 8}, {5, 17}, {9, 29}, {13, 42}, {18, 60}, {24, 80}, {33, 106}, {47, 183}};
+
+static int decode_etc1(const uint8_t blk[8], uint8_t out[64])
+{
+    const uint32_t w0 = (uint32_t)blk[0] << 24 | (uint32_t)blk[1] << 16 | (uint32_t)blk[2] << 8 | blk[3];
+    const uint32_t w1 = (uint32_t)blk[4] << 24 | (uint32_t)blk[5] << 16 | (uint32_t)blk[6] << 8 | blk[7];
+    const int diff = (w0 >> 1) & 1, flip = w0 & 1;
+    int base[2][3];
+    if (diff) { /* 5-bit colour + signed 3-bit delta, decoder.cpp:554-631 */
+        for (int c = 0; c < 3; ++c) {
+            const int c5 = (w0 >> (27 - 8 * c)) & 31;
+            int d = (w0 >> (24 - 8 * c)) & 7;
+            d = d >= 4 ? d - 8 : d;
+            const int c52 = c5 + d;
+            if (c52 < 0 || c52 > 31) {  /* an ETC2 mode: not decoded here, zeros */
+                memset(out, 0, 64);
+                return -1;
+            }
+            base[0][c] = c5 << 3 | c5 >> 2;
+            base[1][c] = c52 << 3 | c52 >> 2;
+        }
+    } else { /* two 4-bit colours, decoder.cpp:412-424 */
+        for (int c = 0; c < 3; ++c) {
+            const int a = (w0 >> (28 - 8 * c)) & 15, b = (w0 >> (24 - 8 * c)) & 15;
+            base[0][c] = a << 4 | a;
+            base[1][c] = b << 4 | b;
+        }
+    }
+    const int table[2] = {(int)(w0 >> 5) & 7, (int)(w0 >> 2) & 7};
+    for (int y = 0; y < 4; ++y)
+        for (int x = 0; x < 4; ++x) {
+            const int k = 4 * x + y; /* column-major pixel bit */
+            const int idx = (int)((w1 >> (16 + k)) & 1) << 1 | (int)((w1 >> k) & 1);
+            const int sub = flip ? (y >= 2) : (x >= 2);
+            const int m = etc1_modifiers[table[sub]][idx & 1] * ((idx & 2) ? -1 : 1);
+            uint8_t* px = out + 4 * (4 * y + x);
+            for (int c = 0; c < 3; ++c) {
+                const int v = base[sub][c] + m;
+                px[c] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+            }
+            px[3] = 255;
+        }
+    return 0;
+}
+
+int oracle_decode_block(int codec, const uint8_t blk[8], uint8_t out[64])
+{
+    if (codec == ORACLE_BC1) {
+        decode_bc1(blk, out);
+        return 0;
+    }
+    return decode_etc1(blk, out);
+}
+
+long oracle_decode_image(int codec, const uint8_t* blocks, unsigned width, unsigned height, uint8_t* rgba,
+                         unsigned stride)
+{
+    long bad = 0;
+    uint8_t px[64];
+    const unsigned bw = width / 4, bh = height / 4;
+    for (unsigned by = 0; by < bh; ++by)
+        for (unsigned bx = 0; bx < bw; ++bx) {
+            bad += oracle_decode_block(codec, blocks + 8 * ((size_t)by * bw + bx), px) != 0;
+            for (int y = 0; y < 4; ++y) memcpy(rgba + (size_t)(4 * by + y) * stride + 16 * (size_t)bx, px + 16 * y, 16);
+        }
+    return bad;
+}
+
+void oracle_sq_error(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsigned b_stride, unsigned width,
+                     unsigned height, uint64_t sums[4])
+{
+    for (int c = 0; c < 4; ++c) sums[c] = 0;
+    for (unsigned y = 0; y < height; ++y) {
+        const uint8_t* pa = a + (size_t)y * a_stride;
+        const uint8_t* pb = b + (size_t)y * b_stride;
+        for (unsigned x = 0; x < 4 * width; ++x) {
+            const int d = (int)pa[x] - (int)pb[x];
+            sums[x & 3] += (uint64_t)(d * d);
+        }
+    }
+}
+
+double oracle_psnr_rgb(const uint64_t sums[4], unsigned width, unsigned height)
+{
+    /* mseRGB = sum(dR^2 + dG^2 + dB^2) / pixels; psnr = 10 log10(768^2 / mse), DBL_MAX below 1e-7 */
+    const double mse = (double)(sums[0] + sums[1] + sums[2]) / ((double)width * (double)height);
+    if (mse < 0.0000001) return DBL_MAX;
+    return 10.0 * log10((768.0 * 768.0) / mse);
 }

@@ -46,6 +46,30 @@ int oracle_compress_any(int codec, uint8_t* result, const uint8_t* input,
 int oracle_compress_mt(int codec, uint8_t* result, const uint8_t* input,
                        unsigned width, unsigned height, unsigned stride, int threads);
 
+/* ---- decode and error (the reference's quality check) ---------------------
+ * Decode one 8-byte block into 16 RGBA8 pixels (row-major, 64 bytes).
+ * BC1: both endpoint orders (4-colour and 3-colour + transparent black), as
+ * Src/decoder.cpp:799-871 (DecompressColour) + :933-943 (decodeBlockDXT1).
+ * ETC1: individual and differential modes with flip, alpha 255, as
+ * Src/decoder.cpp:388-678 (decompressBlockDiffFlipC) + :958-971.  A
+ * differential block whose second colour leaves 0..31 is an ETC2 mode
+ * (decoder.cpp:740-760); those decode to zeros and return -1, else 0. */
+int oracle_decode_block(int codec, const uint8_t blk[8], uint8_t out[64]);
+
+/* Decode a whole image (width, height multiples of 4) into RGBA8 rows of
+ * `stride` bytes.  Returns the number of unsupported ETC1 blocks. */
+long oracle_decode_image(int codec, const uint8_t* blocks, unsigned width, unsigned height, uint8_t* rgba,
+                         unsigned stride);
+
+/* Per-channel sums of squared differences between two RGBA8 images (bytes 0..3
+ * of each pixel), the integer core of getMsePsnr (Src/main.cpp:403-469). */
+void oracle_sq_error(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsigned b_stride, unsigned width,
+                     unsigned height, uint64_t sums[4]);
+
+/* RGB PSNR exactly as getMsePsnr / getPSNR compute psnrRGB (peak 768,
+ * Src/main.cpp:386-395, :455, :466) from the sums above. */
+double oracle_psnr_rgb(const uint64_t sums[4], unsigned width, unsigned height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,6 +8,8 @@
 // included in this one translation unit only.
 #include "goofy_tc.h"
 
+#include "decoder.h"
+
 #include <thread>
 #include <vector>
 
@@ -41,4 +43,12 @@ extern "C" int ref_compress_mt(int codec, unsigned char* result, const unsigned 
     }
     for (auto& th : pool) th.join();
     return threads;
+}
+
+// The reference harness's block decoders (Src/decoder.cpp:933-971): one
+// block into 16 RGBA8 pixels, 16-byte rows.
+extern "C" void ref_decode_block(int codec, const unsigned char* blk, unsigned char* out64)
+{
+    if (codec == 0) DecoderBC::decodeBlockDXT1(blk, out64, 16);
+    else DecoderBC::decodeBlockETC1(blk, out64, 16);
 }
