@@ -9,8 +9,8 @@
 // modes, both flips; ETC2-only differential overflows are counted as
 // unsupported and decoded as black) and either stores the 16 pixels or
 // compares them with the source pixels, summing squared differences per
-// channel exactly in integers (warp shuffles, then one 64-bit atomic per warp
-// and channel).
+// channel exactly in integers (64-bit per thread over a grid stride, then
+// shuffles and shared memory, one 64-bit atomic per CTA and channel).
 #include <cuda_runtime.h>
 
 #include "block_codec.cuh"
@@ -171,40 +171,45 @@ __device__ __forceinline__ void accumulate_row(const uint32_t (&a)[4], const uin
     for (int c = 0; c < 4; ++c) acc[c] = __dp4a(ch[c], ch[c], acc[c]);
 }
 
+// Resident grid: each thread walks blocks with a grid stride, keeps 64-bit
+// sums, then the CTA reduces (shuffles, shared memory) and adds its five
+// totals with one atomic each.
 template <int CODEC>
 __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
                                                           uint32_t nblk, const uint8_t* __restrict__ src,
                                                           size_t stride, bool vec16,
                                                           unsigned long long* __restrict__ sums)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
-    bool ok = true;
-    if (i < nblk) {
+    unsigned long long s[5] = {0, 0, 0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
         const uint32_t by = i / bw, bx = i - by * bw;
         uint32_t px[16], w[16];
-        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
+        const bool ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
         load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
+        uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
             const uint32_t a[4] = {w[4 * y], w[4 * y + 1], w[4 * y + 2], w[4 * y + 3]};
             const uint32_t b[4] = {px[4 * y], px[4 * y + 1], px[4 * y + 2], px[4 * y + 3]};
             accumulate_row(a, b, acc);
         }
-    }
-    unsigned long long s[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        s[c] = acc[c];
+        for (int c = 0; c < 4; ++c) s[c] += acc[c];
+        s[4] += ok ? 0u : 1u;
+    }
+    __shared__ unsigned long long part[5][8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+        if (lane == 0) part[c][warp] = s[c];
     }
-    const unsigned bad = __ballot_sync(0xffffffffu, !ok);
-    if ((threadIdx.x & 31u) == 0) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-            if (s[c]) atomicAdd(&sums[c], s[c]);
-        if (bad) atomicAdd(&sums[4], (unsigned long long)__popc(bad));
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        unsigned long long t = 0;
+        for (uint32_t k = 0; k < (blockDim.x >> 5); ++k) t += part[threadIdx.x][k];
+        if (t) atomicAdd(&sums[threadIdx.x], t);
     }
 }
 
@@ -224,7 +229,10 @@ cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* 
 {
     const uint32_t bw = width / 4, nblk = bw * (height / 4);
     if (nblk == 0) return cudaSuccess;
-    const uint32_t grid = (nblk + 255) / 256;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t grid = min((nblk + 255) / 256, (uint32_t)(sms > 0 ? sms : 1) * 8u);
     if (codec == kBC1)
         block_error_kernel<kBC1><<<grid, 256, 0, stream>>>(blocks, bw, nblk, src, stride, vec16, sums);
     else
