@@ -124,6 +124,8 @@ def _declare(lib):
         "goofy_gpu_block_error_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
         "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
                                               ctypes.POINTER(ctypes.c_double), _VP]),
+        "goofy_gpu_container_size": (ctypes.c_size_t, [ctypes.c_int, _VP, _VP, _U32]),
+        "goofy_gpu_write_container": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _VP, _U32, _VP, ctypes.c_size_t]),
         "goofy_gpu_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
         "goofy_gpu_server_create": (ctypes.c_int, [ctypes.POINTER(_VP), ctypes.POINTER(ServerConfig)]),
         "goofy_gpu_server_destroy": (None, [_VP]),
@@ -449,3 +451,22 @@ def psnr_rgb(codec, blocks, src, width, height, stride):
     rc = lib().goofy_gpu_psnr_rgb(codec, _addr(blocks), _addr(src), width, height, stride, ctypes.byref(out),
                                   sums.ctypes.data)
     return rc, out.value, sums
+
+
+def container(codec, levels):
+    """DDS (BC1) / KTX (ETC1s) file bytes from [(blocks, width, height), ...] host levels."""
+    import numpy as np
+
+    n = len(levels)
+    blocks = [np.ascontiguousarray(b, dtype=np.uint8) for b, _, _ in levels]
+    ptrs = (ctypes.c_void_p * n)(*[b.ctypes.data for b in blocks])
+    ws = (ctypes.c_uint32 * n)(*[w for _, w, _ in levels])
+    hs = (ctypes.c_uint32 * n)(*[h for _, _, h in levels])
+    size = lib().goofy_gpu_container_size(codec, ws, hs, n)
+    if size == 0:
+        raise ValueError("invalid container levels")
+    out = np.zeros(size, np.uint8)
+    rc = lib().goofy_gpu_write_container(codec, ptrs, ws, hs, n, out.ctypes.data, size)
+    if rc != OK:
+        raise RuntimeError(status_string(rc))
+    return out.tobytes()

@@ -146,6 +146,19 @@ int goofy_gpu_block_error_device(int codec, const void* blocks, const void* src,
 int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
                        uint32_t stride, double* psnr_rgb, uint64_t* sums_out);
 
+/* ---- containers ---------------------------------------------------------------- */
+
+/* Bytes of the container of `levels` levels (host blocks): DDS for BC1, KTX
+ * 1.1 for ETC1s.  0 for invalid arguments. */
+size_t goofy_gpu_container_size(int codec, const uint32_t* widths, const uint32_t* heights, uint32_t levels);
+
+/* Write header + levels into `out`: DDS ("DXT1" FourCC) for BC1, KTX 1.1
+ * (GL_ETC1_RGB8_OES) for ETC1s.  With one level the bytes equal the
+ * reference harness's saveDds / saveKtx output (Src/main.cpp:154-220);
+ * several levels form a mip chain (level 0 first). */
+int goofy_gpu_write_container(int codec, const uint8_t* const* level_blocks, const uint32_t* widths,
+                              const uint32_t* heights, uint32_t levels, uint8_t* out, size_t out_size);
+
 /* ---- batches: many device images of uneven sizes in one launch ----------- */
 
 /* One image of a batch (a texture or one of its mip levels).  src / dst and
