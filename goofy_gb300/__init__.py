@@ -75,6 +75,11 @@ class ServerStats(ctypes.Structure):
                 ("max_batch", ctypes.c_uint64), ("waiting", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64)]
 
 
+class Level(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("stride", ctypes.c_uint32)]
+
+
 class Tile(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
                 ("persistent", ctypes.c_uint32)]
@@ -124,6 +129,10 @@ def _declare(lib):
         "goofy_gpu_block_error_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
         "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
                                               ctypes.POINTER(ctypes.c_double), _VP]),
+        "goofy_gpu_mip_count": (_U32, [_U32, _U32]),
+        "goofy_gpu_mip_arena_bytes": (ctypes.c_size_t, [_U32, _U32]),
+        "goofy_gpu_generate_mips": (ctypes.c_int, [_VP, _U32, _U32, _U32, _VP, ctypes.c_size_t, ctypes.POINTER(Level),
+                                                   _U32, ctypes.POINTER(_U32), _VP]),
         "goofy_gpu_container_size": (ctypes.c_size_t, [ctypes.c_int, _VP, _VP, _U32]),
         "goofy_gpu_write_container": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _VP, _U32, _VP, ctypes.c_size_t]),
         "goofy_gpu_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
@@ -470,3 +479,15 @@ def container(codec, levels):
     if rc != OK:
         raise RuntimeError(status_string(rc))
     return out.tobytes()
+
+
+def generate_mips(src, width, height, stride, arena, arena_bytes, stream=None):
+    """Device mip chain of `src` into `arena`; returns [(ptr, w, h, stride), ...] (level 0 = src)."""
+    n = lib().goofy_gpu_mip_count(width, height)
+    levels = (Level * max(n, 1))()
+    count = ctypes.c_uint32()
+    rc = lib().goofy_gpu_generate_mips(_addr(src), width, height, stride, _addr(arena), arena_bytes, levels,
+                                       max(n, 1), ctypes.byref(count), stream)
+    if rc != OK:
+        raise RuntimeError("generate_mips: %s %s" % (status_string(rc), last_error()))
+    return [(levels[i].data, levels[i].width, levels[i].height, levels[i].stride) for i in range(count.value)]

@@ -146,6 +146,30 @@ int goofy_gpu_block_error_device(int codec, const void* blocks, const void* src,
 int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
                        uint32_t stride, double* psnr_rgb, uint64_t* sums_out);
 
+/* ---- mip chains on the device -------------------------------------------------- */
+
+/* One level of a mip chain on the device. */
+typedef struct goofy_gpu_level {
+    void* data;
+    uint32_t width, height, stride;
+} goofy_gpu_level;
+
+/* Levels of the chain of a width x height texture (each axis halves,
+ * clamped at 4, down to 4x4); 0 unless both sizes are powers of two >= 4. */
+uint32_t goofy_gpu_mip_count(uint32_t width, uint32_t height);
+
+/* Device bytes goofy_gpu_generate_mips needs for levels 1.. (256-byte rows). */
+size_t goofy_gpu_mip_arena_bytes(uint32_t width, uint32_t height);
+
+/* Build levels 1.. of the chain of `src` (device RGBA8) into `arena`
+ * (device, 256-byte aligned) with a 2x2 box filter with rounding,
+ * (a+b+c+d+2)>>2 per channel (an axis already at 4 is copied), and describe
+ * all levels (levels[0] = src) for goofy_gpu_batch_encode.  No reference
+ * counterpart (the reference encodes levels the caller made).  Async. */
+int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32_t height, uint32_t stride, void* arena,
+                            size_t arena_bytes, goofy_gpu_level* levels, uint32_t max_levels, uint32_t* nlevels,
+                            void* stream);
+
 /* ---- containers ---------------------------------------------------------------- */
 
 /* Bytes of the container of `levels` levels (host blocks): DDS for BC1, KTX
