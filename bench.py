@@ -597,7 +597,7 @@ def run_gpu(args):
     # quality: RGB PSNR of the timed outputs (the reference harness's secondary
     # metric), and the speed of the fused decode + squared-error kernel
     quality = {}
-    d_sums = torch.zeros(5, dtype=torch.int64, device=dev)
+    d_sums = torch.zeros(6, dtype=torch.int64, device=dev)
     for c in codecs:
         rc, psnr, sums = g.psnr_rgb(c, dst[c], src[c], W, H, 4 * W)
         assert rc == g.OK, g.last_error()

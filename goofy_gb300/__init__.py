@@ -80,6 +80,13 @@ class Level(ctypes.Structure):
                 ("stride", ctypes.c_uint32)]
 
 
+class Quality(ctypes.Structure):
+    """goofy_gpu_quality: the harness's MsePsnr record."""
+    _fields_ = [(n, ctypes.c_double) for n in ("mse_r", "mse_g", "mse_b", "mse_a", "mse_max", "mse_rgb", "mse_y",
+                                                "psnr_r", "psnr_g", "psnr_b", "psnr_a", "psnr_min", "psnr_rgb",
+                                                "psnr_y")] + [("unsupported_blocks", ctypes.c_uint64)]
+
+
 class Tile(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
                 ("persistent", ctypes.c_uint32)]
@@ -129,6 +136,10 @@ def _declare(lib):
         "goofy_gpu_block_error_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
         "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
                                               ctypes.POINTER(ctypes.c_double), _VP]),
+        "goofy_gpu_mse_psnr": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, ctypes.POINTER(Quality)]),
+        "goofy_gpu_png_info": (ctypes.c_int, [_VP, ctypes.c_size_t, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
+        "goofy_gpu_png_decode": (ctypes.c_int, [_VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _U32, ctypes.c_int,
+                                                ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
         "goofy_gpu_mip_count": (_U32, [_U32, _U32]),
         "goofy_gpu_mip_arena_bytes": (ctypes.c_size_t, [_U32, _U32]),
         "goofy_gpu_generate_mips": (ctypes.c_int, [_VP, _U32, _U32, _U32, _VP, ctypes.c_size_t, ctypes.POINTER(Level),
@@ -446,7 +457,13 @@ def decode_device(codec, rgba, rgba_stride, blocks, width, height, d_unsupported
                                          _addr(d_unsupported), stream)
 
 
+ERROR_SUMS = 6  # device accumulators goofy_gpu_block_error_device adds to
+
+
 def block_error_device(codec, blocks, src, width, height, stride, d_sums, stream=None):
+    """Adds the six error sums (see goofy_gpu_block_error_device) to device uint64[6] `d_sums`."""
+    if hasattr(d_sums, "numel") and d_sums.numel() * d_sums.element_size() < 8 * ERROR_SUMS:
+        raise ValueError("d_sums must hold %d uint64 accumulators" % ERROR_SUMS)
     return lib().goofy_gpu_block_error_device(codec, _addr(blocks), _addr(src), width, height, stride,
                                               _addr(d_sums), stream)
 
@@ -460,6 +477,16 @@ def psnr_rgb(codec, blocks, src, width, height, stride):
     rc = lib().goofy_gpu_psnr_rgb(codec, _addr(blocks), _addr(src), width, height, stride, ctypes.byref(out),
                                   sums.ctypes.data)
     return rc, out.value, sums
+
+
+def mse_psnr(codec, blocks, src, width, height, stride):
+    """The harness's getMsePsnr of device `src` against its decoded device
+    `blocks`, computed on the GPU; a dict of the MsePsnr fields."""
+    q = Quality()
+    rc = lib().goofy_gpu_mse_psnr(codec, _addr(blocks), _addr(src), width, height, stride, ctypes.byref(q))
+    if rc != OK:
+        raise RuntimeError("mse_psnr: %s %s" % (status_string(rc), last_error()))
+    return {n: getattr(q, n) for n, _ in Quality._fields_}
 
 
 def container(codec, levels):
@@ -491,3 +518,23 @@ def generate_mips(src, width, height, stride, arena, arena_bytes, stream=None):
     if rc != OK:
         raise RuntimeError("generate_mips: %s %s" % (status_string(rc), last_error()))
     return [(levels[i].data, levels[i].width, levels[i].height, levels[i].stride) for i in range(count.value)]
+
+
+def read_png(source, opaque=True, stride=None):
+    """Decode a PNG (path or bytes) with the library's decoder into a numpy
+    RGBA8 image of shape (height, stride); returns (image, width, height)."""
+    import numpy as np
+
+    data = source if isinstance(source, (bytes, bytearray)) else open(source, "rb").read()
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    w, h = _U32(), _U32()
+    rc = lib().goofy_gpu_png_info(buf, len(data), ctypes.byref(w), ctypes.byref(h))
+    if rc != OK:
+        raise ValueError("png: %s %s" % (status_string(rc), last_error()))
+    stride = stride or 4 * w.value
+    img = np.zeros((h.value, stride), np.uint8)
+    rc = lib().goofy_gpu_png_decode(buf, len(data), img.ctypes.data, img.nbytes, stride, 1 if opaque else 0,
+                                    ctypes.byref(w), ctypes.byref(h))
+    if rc != OK:
+        raise ValueError("png: %s %s" % (status_string(rc), last_error()))
+    return img, w.value, h.value

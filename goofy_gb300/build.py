@@ -35,7 +35,7 @@ def _cuda_home():
 
 
 CU_SOURCES = ["encode_kernels.cu", "batch_kernels.cu", "batch_noalloc.cu", "decode_kernels.cu", "mips.cu"]
-CPP_SOURCES = ["capi.cpp", "batch.cpp", "server.cpp", "server_replay.cpp", "quality.cpp", "containers.cpp"]
+CPP_SOURCES = ["capi.cpp", "batch.cpp", "server.cpp", "server_replay.cpp", "quality.cpp", "containers.cpp", "png.cpp"]
 HEADERS = ["block_codec.cuh", "device_io.cuh", "kernels.h", "batch.h", "host_util.h", "decode.h"]
 
 

@@ -171,8 +171,24 @@ __device__ __forceinline__ void accumulate_row(const uint32_t (&a)[4], const uin
     for (int c = 0; c < 4; ++c) acc[c] = __dp4a(ch[c], ch[c], acc[c]);
 }
 
+// The harness's luminosity difference (0.21 R + 0.72 G + 0.07 B of a pixel
+// read as a little-endian u32, R = byte 2) in hundredths, which is exact in
+// integers: 21 * d(byte 2) + 72 * d(byte 1) + 7 * d(byte 0); squared and
+// summed over a row of 4 pixels (at most 4 * 25500^2 < 2^32).
+__device__ __forceinline__ uint32_t luma_row(const uint32_t (&a)[4], const uint32_t (&b)[4])
+{
+    constexpr uint32_t kWeights = 0x00154807u;  // bytes 0..3: 7, 72, 21, 0
+    uint32_t acc = 0;
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+        const int d = (int)__dp4a(a[x], kWeights, 0u) - (int)__dp4a(b[x], kWeights, 0u);
+        acc += (uint32_t)(d * d);
+    }
+    return acc;
+}
+
 // Resident grid: each thread walks blocks with a grid stride, keeps 64-bit
-// sums, then the CTA reduces (shuffles, shared memory) and adds its five
+// sums, then the CTA reduces (shuffles, shared memory) and adds its six
 // totals with one atomic each.
 template <int CODEC>
 __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
@@ -180,7 +196,7 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
                                                           size_t stride, bool vec16,
                                                           unsigned long long* __restrict__ sums)
 {
-    unsigned long long s[5] = {0, 0, 0, 0, 0};
+    unsigned long long s[6] = {0, 0, 0, 0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
         const uint32_t by = i / bw, bx = i - by * bw;
         uint32_t px[16], w[16];
@@ -192,21 +208,22 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
             const uint32_t a[4] = {w[4 * y], w[4 * y + 1], w[4 * y + 2], w[4 * y + 3]};
             const uint32_t b[4] = {px[4 * y], px[4 * y + 1], px[4 * y + 2], px[4 * y + 3]};
             accumulate_row(a, b, acc);
+            s[5] += luma_row(a, b);
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c) s[c] += acc[c];
         s[4] += ok ? 0u : 1u;
     }
-    __shared__ unsigned long long part[5][8];
+    __shared__ unsigned long long part[6][8];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int c = 0; c < 5; ++c) {
+    for (int c = 0; c < 6; ++c) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
         if (lane == 0) part[c][warp] = s[c];
     }
     __syncthreads();
-    if (threadIdx.x < 5) {
+    if (threadIdx.x < 6) {
         unsigned long long t = 0;
         for (uint32_t k = 0; k < (blockDim.x >> 5); ++k) t += part[threadIdx.x][k];
         if (t) atomicAdd(&sums[threadIdx.x], t);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cfloat>
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -25,7 +26,7 @@ int check(int codec, const void* a, const void* b, uint32_t width, uint32_t heig
 }
 
 std::mutex g_mu;
-unsigned long long* g_sums[64] = {};  // per device: 5 accumulators of goofy_gpu_psnr_rgb
+unsigned long long* g_sums[64] = {};  // per device: the 6 accumulators of the synchronous quality calls
 
 }  // namespace
 
@@ -64,8 +65,17 @@ GOOFY_EXPORT int goofy_gpu_block_error_device(int codec, const void* blocks, con
     return GOOFY_OK;
 }
 
-GOOFY_EXPORT int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
-                                    uint32_t stride, double* psnr_rgb, uint64_t* sums_out)
+}  // extern "C"
+
+namespace {
+
+// getPSNR, Src/main.cpp:386-395
+double psnr_of(double mse, double peak) { return mse < 0.0000001 ? DBL_MAX : 10.0 * std::log10((peak * peak) / mse); }
+
+// Runs the error kernel on the current device into a library-owned
+// accumulator and reads the six sums back.
+int error_sums(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height, uint32_t stride,
+               unsigned long long h[6])
 {
     int rc = check(codec, blocks, src, width, height);
     if (rc <= 0) return rc == GOOFY_OK ? GOOFY_ERR_INVALID : rc;
@@ -73,19 +83,59 @@ GOOFY_EXPORT int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* s
     GOOFY_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return GOOFY_ERR_NO_DEVICE;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_sums[dev]) GOOFY_CUDA_TRY(cudaMalloc(&g_sums[dev], 5 * sizeof(unsigned long long)));
+    if (!g_sums[dev]) GOOFY_CUDA_TRY(cudaMalloc(&g_sums[dev], 6 * sizeof(unsigned long long)));
     cudaStream_t st = nullptr;
-    GOOFY_CUDA_TRY(cudaMemsetAsync(g_sums[dev], 0, 5 * sizeof(unsigned long long), st));
+    GOOFY_CUDA_TRY(cudaMemsetAsync(g_sums[dev], 0, 6 * sizeof(unsigned long long), st));
     rc = goofy_gpu_block_error_device(codec, blocks, src, width, height, stride,
                                       reinterpret_cast<uint64_t*>(g_sums[dev]), st);
     if (rc != GOOFY_OK) return rc;
-    unsigned long long h[5];
-    GOOFY_CUDA_TRY(cudaMemcpy(h, g_sums[dev], sizeof h, cudaMemcpyDeviceToHost));
+    GOOFY_CUDA_TRY(cudaMemcpy(h, g_sums[dev], 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    return GOOFY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GOOFY_EXPORT int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
+                                    uint32_t stride, double* psnr_rgb, uint64_t* sums_out)
+{
+    unsigned long long h[6];
+    const int rc = error_sums(codec, blocks, src, width, height, stride, h);
+    if (rc != GOOFY_OK) return rc;
     if (sums_out)
         for (int i = 0; i < 5; ++i) sums_out[i] = h[i];
-    // getPSNR(mseRGB, 768), Src/main.cpp:386-395 and :455, :466
+    // getPSNR(mseRGB, 768), Src/main.cpp:455, :466
     const double mse = (double)(h[0] + h[1] + h[2]) / ((double)width * (double)height);
-    if (psnr_rgb) *psnr_rgb = mse < 0.0000001 ? DBL_MAX : 10.0 * std::log10((768.0 * 768.0) / mse);
+    if (psnr_rgb) *psnr_rgb = psnr_of(mse, 768.0);
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_mse_psnr(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
+                                    uint32_t stride, goofy_gpu_quality* out)
+{
+    if (!out) return GOOFY_ERR_INVALID;
+    unsigned long long h[6];
+    const int rc = error_sums(codec, blocks, src, width, height, stride, h);
+    if (rc != GOOFY_OK) return rc;
+    // Src/main.cpp:456-468; the harness's r is byte 2 and its b byte 0
+    const double n = (double)(uint32_t)(width * height);
+    goofy_gpu_quality& r = *out;
+    r.mse_r = (double)h[2] / n;
+    r.mse_g = (double)h[1] / n;
+    r.mse_b = (double)h[0] / n;
+    r.mse_a = (double)h[3] / n;
+    r.mse_rgb = (double)(h[0] + h[1] + h[2]) / n;
+    r.mse_y = (double)h[5] / 10000.0 / n;
+    r.mse_max = std::max(std::max(r.mse_r, r.mse_g), std::max(r.mse_b, r.mse_a));
+    r.psnr_r = psnr_of(r.mse_r, 255.0);
+    r.psnr_g = psnr_of(r.mse_g, 255.0);
+    r.psnr_b = psnr_of(r.mse_b, 255.0);
+    r.psnr_a = psnr_of(r.mse_a, 255.0);
+    r.psnr_min = std::min(std::min(r.psnr_r, r.psnr_g), std::min(r.psnr_b, r.psnr_a));
+    r.psnr_rgb = psnr_of(r.mse_rgb, 768.0);
+    r.psnr_y = psnr_of(r.mse_y, 255.0);
+    r.unsupported_blocks = h[4];
     return GOOFY_OK;
 }
 

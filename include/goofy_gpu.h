@@ -133,18 +133,37 @@ int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, ui
 int goofy_gpu_decode_device(int codec, void* rgba, uint32_t rgba_stride, const void* blocks, uint32_t width,
                             uint32_t height, uint64_t* d_unsupported, void* stream);
 
-/* Adds to d_sums[0..3] (device uint64) the per-channel sums of squared
- * differences between `src` (RGBA8, 4-byte aligned rows) and its decoded
- * `blocks`, and to d_sums[4] the unsupported-block count: the integer core
- * of the reference's getMsePsnr (Src/main.cpp:403-469).  Asynchronous. */
+/* Adds to d_sums[0..5] (device uint64) the integer core of the reference's
+ * getMsePsnr (Src/main.cpp:403-469) between `src` (RGBA8, 4-byte aligned
+ * rows) and its decoded `blocks`: [0..3] per-byte sums of squared
+ * differences, [4] the unsupported-block count, [5] the sum of squared
+ * luminosity differences in hundredths, (21 d2 + 72 d1 + 7 d0)^2 with dk the
+ * difference of byte k -- the harness's 0.21 R + 0.72 G + 0.07 B of a pixel
+ * read as a little-endian u32, exact in integers.  Asynchronous. */
 int goofy_gpu_block_error_device(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
                                  uint32_t stride, uint64_t* d_sums, void* stream);
 
 /* Synchronous convenience: RGB PSNR (peak 768, as the reference reports it)
  * of `blocks` against `src`, both on the current device; sums_out (may be
- * NULL) receives the five accumulators. */
+ * NULL) receives accumulators [0..4] above. */
 int goofy_gpu_psnr_rgb(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
                        uint32_t stride, double* psnr_rgb, uint64_t* sums_out);
+
+/* The harness's MsePsnr record (Src/main.cpp:366-384), same field meaning and
+ * channel naming (a pixel read as a little-endian u32: r = byte 2, b = byte 0). */
+typedef struct goofy_gpu_quality {
+    double mse_r, mse_g, mse_b, mse_a, mse_max, mse_rgb, mse_y;
+    double psnr_r, psnr_g, psnr_b, psnr_a, psnr_min, psnr_rgb, psnr_y;
+    uint64_t unsupported_blocks;
+} goofy_gpu_quality;
+
+/* Synchronous: getMsePsnr(src, decode(blocks)) computed on the current device.
+ * Every MSE except mse_y equals the harness's double result exactly (its sums
+ * are exact integers); mse_y differs only by the harness's own rounding of
+ * its 0.21 / 0.72 / 0.07 products (relative < 1e-10 on its test photographs,
+ * far below the 5 decimals it prints). */
+int goofy_gpu_mse_psnr(int codec, const void* blocks, const void* src, uint32_t width, uint32_t height,
+                       uint32_t stride, goofy_gpu_quality* out);
 
 /* ---- mip chains on the device -------------------------------------------------- */
 
@@ -169,6 +188,24 @@ size_t goofy_gpu_mip_arena_bytes(uint32_t width, uint32_t height);
 int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32_t height, uint32_t stride, void* arena,
                             size_t arena_bytes, goofy_gpu_level* levels, uint32_t max_levels, uint32_t* nlevels,
                             void* stream);
+
+/* ---- PNG ingest (host) ------------------------------------------------------------
+ * Replaces the harness's image loader, loadPngAsRgba8 (Src/main.cpp:258-342:
+ * lodepng::decode to 8-bit RGBA, alpha then forced to 255).  Every colour type
+ * and bit depth and both interlace methods; CRCs and Adler-32 verified; 16-bit
+ * samples keep their high byte, 1/2/4-bit grey scales by 255/(2^depth-1),
+ * tRNS gives alpha 0 to the key colour (lodepng's conversion rules).
+ * GOOFY_ERR_INVALID for a malformed file (text in goofy_gpu_last_error()). */
+
+/* Width and height from the IHDR chunk. */
+int goofy_gpu_png_info(const void* png, size_t png_bytes, uint32_t* width, uint32_t* height);
+
+/* Decode into RGBA8 rows of `stride` bytes (host memory, `rgba_bytes` long);
+ * `opaque` != 0 sets every alpha to 255 as the harness does.  width / height
+ * (may be NULL) receive the image size even when the buffer is too small
+ * (GOOFY_ERR_TOO_LARGE). */
+int goofy_gpu_png_decode(const void* png, size_t png_bytes, void* rgba, size_t rgba_bytes, uint32_t stride,
+                         int opaque, uint32_t* width, uint32_t* height);
 
 /* ---- containers ---------------------------------------------------------------- */
 

@@ -38,6 +38,8 @@ def load():
         lib.oracle_decode_image.argtypes = [ctypes.c_int, _VP, _U, _U, _VP, _U]
         lib.oracle_sq_error.restype = None
         lib.oracle_sq_error.argtypes = [_VP, _U, _VP, _U, _U, _U, _VP]
+        lib.oracle_mse_psnr.restype = None
+        lib.oracle_mse_psnr.argtypes = [_VP, _U, _VP, _U, _U, _U, _VP]
         lib.oracle_psnr_rgb.restype = ctypes.c_double
         lib.oracle_psnr_rgb.argtypes = [_VP, _U, _U]
         _oracle = lib
@@ -55,6 +57,9 @@ def load_ref():
         lib.ref_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
         lib.ref_decode_block.restype = None
         lib.ref_decode_block.argtypes = [ctypes.c_int, _VP, _VP]
+        lib.ref_png_decode.restype = ctypes.c_uint
+        lib.ref_png_decode.argtypes = [_VP, ctypes.c_size_t, _VP, ctypes.c_size_t, ctypes.POINTER(_U),
+                                       ctypes.POINTER(_U)]
         _ref = lib
     return _ref
 
@@ -97,8 +102,38 @@ def sq_error(a, b, width, height):
     return sums
 
 
+MSE_PSNR_FIELDS = ("mse_r", "mse_g", "mse_b", "mse_a", "mse_max", "mse_rgb", "mse_y",
+                   "psnr_r", "psnr_g", "psnr_b", "psnr_a", "psnr_min", "psnr_rgb", "psnr_y")
+
+
+def mse_psnr(a, b, width, height):
+    """The harness's getMsePsnr of two RGBA8 images, as a dict."""
+    import numpy as np
+
+    out = np.zeros(14, np.float64)
+    load().oracle_mse_psnr(a.ctypes.data, a.strides[0], b.ctypes.data, b.strides[0], width, height, out.ctypes.data)
+    return dict(zip(MSE_PSNR_FIELDS, out.tolist()))
+
+
 def psnr_rgb(sums, width, height):
     import numpy as np
 
     s = np.ascontiguousarray(sums, dtype=np.uint64)
     return load().oracle_psnr_rgb(s.ctypes.data, width, height)
+
+
+def ref_png_decode(data, max_pixels=1 << 26):
+    """The harness's PNG loader (lodepng::decode to RGBA8) on PNG bytes:
+    (error, rgba rows (h, 4w), w, h); None without the reference library."""
+    import numpy as np
+
+    lib = load_ref()
+    if lib is None:
+        return None
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    out = np.zeros(4 * max_pixels, np.uint8)
+    w, h = _U(), _U()
+    err = lib.ref_png_decode(buf, len(data), out.ctypes.data, out.nbytes, ctypes.byref(w), ctypes.byref(h))
+    if err:
+        return err, None, 0, 0
+    return 0, out[:4 * w.value * h.value].reshape(h.value, 4 * w.value).copy(), w.value, h.value

@@ -18,6 +18,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 REFERENCE_HEADER_DIR = "/root/reference/GoofyTC"
 REFERENCE_SRC_DIR = "/root/reference/Src"
+REFERENCE_PNG_DIR = "/root/reference/ThirdParty/lodepng"
 
 ORACLE_SO = os.path.join(BUILD_DIR, "libgoofy_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libgoofy_ref.so")
@@ -43,14 +44,16 @@ def ref_available():
 
 
 def ref_cmd():
-    """The reference encoder header and the reference harness's decoder
-    (Src/decoder.cpp, compiled from where it lies) behind ref_shim.cpp."""
+    """The reference encoder header, the reference harness's decoder
+    (Src/decoder.cpp) and its PNG loader (ThirdParty/lodepng/lodepng.cpp), all
+    compiled from where they lie, behind ref_shim.cpp."""
     src = os.path.join(HERE, "ref_shim.cpp")
     hdr = os.path.join(REFERENCE_HEADER_DIR, "goofy_tc.h")
     dec = os.path.join(REFERENCE_SRC_DIR, "decoder.cpp")
-    return [src, hdr, dec], [
+    png = os.path.join(REFERENCE_PNG_DIR, "lodepng.cpp")
+    return [src, hdr, dec, png], [
         "g++", "-O3", "-DNDEBUG", "-std=c++17", "-fPIC", "-shared", "-pthread", "-msse2",
-        "-I", REFERENCE_HEADER_DIR, "-I", REFERENCE_SRC_DIR, "-o", REF_SO, src, dec]
+        "-I", REFERENCE_HEADER_DIR, "-I", REFERENCE_SRC_DIR, "-I", REFERENCE_PNG_DIR, "-o", REF_SO, src, dec, png]
 
 
 def build(verbose=False):

@@ -322,6 +322,53 @@ void oracle_sq_error(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsi
     }
 }
 
+static double psnr_of(double mse, double peak)
+{
+    /* getPSNR, Src/main.cpp:386-395 */
+    if (mse < 0.0000001) return DBL_MAX;
+    return 10.0 * log10((peak * peak) / mse);
+}
+
+void oracle_mse_psnr(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsigned b_stride, unsigned width,
+                     unsigned height, double out[14])
+{
+    /* getMsePsnr, Src/main.cpp:403-469, in its own double arithmetic and
+     * order.  Each pixel is read as a little-endian u32, so its "R" is byte 2
+     * and its "B" byte 0 (:423-431); luminosity 0.21 R + 0.72 G + 0.07 B
+     * (:398-401). */
+    double mr = 0, mg = 0, mb = 0, ma = 0, mrgb = 0, my = 0;
+    for (unsigned y = 0; y < height; ++y) {
+        const uint8_t* pa = a + (size_t)y * a_stride;
+        const uint8_t* pb = b + (size_t)y * b_stride;
+        for (unsigned x = 0; x < width; ++x) {
+            const double r1 = pa[4 * x + 2], g1 = pa[4 * x + 1], b1 = pa[4 * x], a1 = pa[4 * x + 3];
+            const double r2 = pb[4 * x + 2], g2 = pb[4 * x + 1], b2 = pb[4 * x], a2 = pb[4 * x + 3];
+            const double y1 = 0.21 * r1 + 0.72 * g1 + 0.07 * b1;
+            const double y2 = 0.21 * r2 + 0.72 * g2 + 0.07 * b2;
+            const double dy = y2 - y1;
+            my += dy * dy;
+            const double dr = r1 - r2, dg = g1 - g2, db = b1 - b2, da = a1 - a2;
+            mrgb += (dr * dr) + (dg * dg) + (db * db);
+            mr += dr * dr;
+            mg += dg * dg;
+            mb += db * db;
+            ma += da * da;
+        }
+    }
+    const double n = (double)(uint32_t)(width * height); /* the harness multiplies in 32 bits */
+    out[0] = mr / n;
+    out[1] = mg / n;
+    out[2] = mb / n;
+    out[3] = ma / n;
+    out[5] = mrgb / n;
+    out[6] = my / n;
+    out[4] = fmax(fmax(out[0], out[1]), fmax(out[2], out[3]));
+    for (int c = 0; c < 4; ++c) out[7 + c] = psnr_of(out[c], 255.0);
+    out[11] = fmin(fmin(out[7], out[8]), fmin(out[9], out[10]));
+    out[12] = psnr_of(out[5], 768.0);
+    out[13] = psnr_of(out[6], 255.0);
+}
+
 double oracle_psnr_rgb(const uint64_t sums[4], unsigned width, unsigned height)
 {
     /* mseRGB = sum(dR^2 + dG^2 + dB^2) / pixels; psnr = 10 log10(768^2 / mse), DBL_MAX below 1e-7 */

@@ -70,6 +70,13 @@ void oracle_sq_error(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsi
  * Src/main.cpp:386-395, :455, :466) from the sums above. */
 double oracle_psnr_rgb(const uint64_t sums[4], unsigned width, unsigned height);
 
+/* The harness's full getMsePsnr (Src/main.cpp:403-469) in its own double
+ * arithmetic, pixel order and channel naming (a pixel read as a little-endian
+ * u32: R = byte 2, B = byte 0).  out = mseR, mseG, mseB, mseA, mseMax, mseRGB,
+ * mseY, psnrR, psnrG, psnrB, psnrA, psnrMin, psnrRGB, psnrY. */
+void oracle_mse_psnr(const uint8_t* a, unsigned a_stride, const uint8_t* b, unsigned b_stride, unsigned width,
+                     unsigned height, double out[14]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,9 @@
 // ref_shim.cpp -- TEST INFRASTRUCTURE: exposes the reference encoder itself
 // (goofy::compressDXT1 / goofy::compressETC1 from GoofyTC/goofy_tc.h, included
 // from the reference tree by oracle/build.py via -I; nothing is copied) with C
-// linkage so tests and the golden-vector script can call it through ctypes.
+// linkage so tests and the golden-vector script can call it through ctypes,
+// together with the harness's block decoders and its PNG loader (lodepng,
+// ThirdParty/lodepng, also compiled from where it lies).
 // It is compiled in the Release configuration (-DNDEBUG) the reference harness
 // ships with; a debug build asserts 64-byte aligned strips (goofy_tc.h:1072).
 // goofy_tc.h defines its functions non-inline (goofy_tc.h:34), so it is
@@ -9,6 +11,7 @@
 #include "goofy_tc.h"
 
 #include "decoder.h"
+#include "lodepng.h"
 
 #include <thread>
 #include <vector>
@@ -51,4 +54,18 @@ extern "C" void ref_decode_block(int codec, const unsigned char* blk, unsigned c
 {
     if (codec == 0) DecoderBC::decodeBlockDXT1(blk, out64, 16);
     else DecoderBC::decodeBlockETC1(blk, out64, 16);
+}
+
+// The harness's PNG loader core (Src/main.cpp:270: lodepng::decode to 8-bit
+// RGBA, from memory here).  Returns lodepng's error code; on success `out`
+// (caller-sized by ref_png_size) receives width*height*4 bytes.
+extern "C" unsigned ref_png_decode(const unsigned char* png, size_t n, unsigned char* out, size_t out_bytes,
+                                   unsigned* w, unsigned* h)
+{
+    std::vector<unsigned char> img;
+    const unsigned err = lodepng::decode(img, *w, *h, png, n);
+    if (err) return err;
+    if (img.size() > out_bytes) return 1000;
+    std::copy(img.begin(), img.end(), out);
+    return 0;
 }

@@ -84,7 +84,29 @@ def test_error_sums_unaligned_source(cuda):
     buf[4:4 + h * stride].reshape(h, stride)[:, :4 * w] = img
     d_buf = cuda.from_numpy(buf).cuda()
     d_blk = cuda.from_numpy(blocks).cuda()
-    sums = cuda.zeros(5, dtype=cuda.int64, device="cuda")
+    sums = cuda.zeros(6, dtype=cuda.int64, device="cuda")
     assert g.block_error_device(1, d_blk, d_buf.data_ptr() + 4, w, h, stride, sums) == g.OK
     cuda.cuda.synchronize()
     np.testing.assert_array_equal(sums.cpu().numpy()[:4].astype(np.uint64), want)
+
+
+@pytest.mark.parametrize("codec", [0, 1])
+def test_full_mse_psnr_record(cuda, codec):
+    """The harness's whole getMsePsnr record (per channel, max / min, RGB,
+    luminosity) measured on the GPU equals the oracle's restatement, which
+    does the harness's own double arithmetic; random alpha makes mse_a non-zero."""
+    rng = np.random.default_rng(3 + codec)
+    for (w, h) in ((256, 256), (1028, 36), (2048, 1024)):
+        img = workloads.scene(w, h, w + codec)
+        img.reshape(h, w, 4)[..., 3] = rng.integers(0, 256, (h, w))
+        blocks = oracle.encode(codec, img, w, h, threads=0)
+        dec, _ = oracle.decode(codec, blocks, w, h)
+        want = oracle.mse_psnr(img, dec, w, h)
+        q = g.mse_psnr(codec, cuda.from_numpy(blocks).cuda(), cuda.from_numpy(np.ascontiguousarray(img).reshape(-1)).cuda(),
+                       w, h, 4 * w)
+        assert q["unsupported_blocks"] == 0
+        for k, v in want.items():
+            if k.endswith("_y"):  # exact integers vs the harness's rounded 0.21 / 0.72 / 0.07 products
+                assert q[k] == pytest.approx(v, rel=1e-10), k
+            else:
+                assert q[k] == v, k

@@ -1,0 +1,59 @@
+"""Real-image regression on the reference's own test photographs (CPU side):
+the committed digests agree with the harness's printed result rows; where the
+photographs are present, the library's PNG loader gives the harness's pixels
+and the oracle gives the reference's blocks and quality numbers on every
+photograph the harness accepts."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import goofy_gb300 as g
+import oracle
+
+DIGESTS = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "photo_digests.json")))
+TEST_DATA = os.environ.get("GOOFY_TEST_DATA", "/root/reference/test-data")
+CODECS = {"DXT1": "bc1", "ETC1": "etc1s"}
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_digests_agree_with_the_harness_output():
+    rows = DIGESTS["harness_rows"]
+    assert {r["format"] for r in rows} == {"DXT1", "ETC1"}
+    for r in rows:
+        q = DIGESTS["photos"][r["image"]][CODECS[r["format"]]]["mse_psnr"]
+        for k in ("mse_r", "mse_g", "mse_b", "mse_max", "mse_rgb", "mse_y", "psnr_r", "psnr_g", "psnr_b", "psnr_min",
+                  "psnr_rgb", "psnr_y"):
+            assert "%3.5f" % q[k] == r[k], (r["image"], r["format"], k)
+
+
+def luma_mse(src, dec, w, h):
+    """mseY from exact integers (what the GPU measurement sums): the harness's 0.21 R + 0.72 G + 0.07 B (R =
+    byte 2 of a little-endian pixel) scaled by 100."""
+    d = src.reshape(h, w, 4)[..., :3].astype(np.int64) - dec.reshape(h, w, 4)[..., :3].astype(np.int64)
+    y = 21 * d[..., 2] + 72 * d[..., 1] + 7 * d[..., 0]
+    return float((y * y).sum()) / 10000.0 / (w * h)
+
+
+@pytest.mark.skipif(not os.path.isdir(TEST_DATA), reason="reference test photographs not present")
+@pytest.mark.parametrize("name", sorted(DIGESTS["photos"]))
+def test_photograph_against_reference_digest(built, name):
+    d = DIGESTS["photos"][name]
+    img, w, h = g.read_png(os.path.join(TEST_DATA, name + ".png"))
+    assert (w, h) == (d["width"], d["height"])
+    assert _sha(img) == d["rgba_sha256"]
+    for codec, cname in enumerate(("bc1", "etc1s")):
+        out = oracle.encode(codec, img, w, h, any_width=False)
+        assert _sha(out) == d[cname]["sha256"]
+        dec, bad = oracle.decode(codec, out, w, h)
+        assert bad == d[cname]["unsupported_blocks"] == 0
+        q = oracle.mse_psnr(img, dec, w, h)
+        for k, v in d[cname]["mse_psnr"].items():
+            assert q[k] == pytest.approx(v, rel=1e-12), k
+        # exact integers vs the harness's rounded 0.21 / 0.72 / 0.07 products
+        assert luma_mse(img, dec, w, h) == pytest.approx(q["mse_y"], rel=1e-10)
