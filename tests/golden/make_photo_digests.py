@@ -12,9 +12,9 @@ For every PNG in the reference's test-data/ that its harness accepts
   and the fourteen getMsePsnr values of that output decoded by the
   harness's decoders (the oracle's restatements, themselves pinned to
   Src/decoder.cpp and to the harness run below);
-* the harness's own result rows for its default image (parrot_red), from
-  one run of the harness compiled from the reference tree
-  (oracle/run_harness.py), as printed (5 decimals).
+* the harness's own result rows (Goofy and its RGB565 baseline) for its
+  default image (parrot_red), from one run of the harness compiled from the
+  reference tree (oracle/run_harness.py), as printed (5 decimals).
 
 Run:  python tests/golden/make_photo_digests.py
 """
@@ -61,7 +61,7 @@ def main():
             entry[cname] = {"sha256": sha(out), "unsupported_blocks": int(bad),
                             "mse_psnr": oracle.mse_psnr(img, dec, w, h)}
         photos[name] = entry
-    harness = [r for r in run_harness.run() if r["encoder"] == "simd_goofy"]
+    harness = [r for r in run_harness.run() if r["encoder"] in ("simd_goofy", "Baseline (Downsample x2)")]
     with open(OUT, "w") as f:
         json.dump({"photos": photos, "harness_rows": harness}, f, indent=1, sort_keys=True)
     print("wrote", OUT, len(photos), "photos,", len(harness), "harness rows")

@@ -23,7 +23,7 @@ def _sha(a):
 
 
 def test_digests_agree_with_the_harness_output():
-    rows = DIGESTS["harness_rows"]
+    rows = [r for r in DIGESTS["harness_rows"] if r["encoder"] == "simd_goofy"]
     assert {r["format"] for r in rows} == {"DXT1", "ETC1"}
     for r in rows:
         q = DIGESTS["photos"][r["image"]][CODECS[r["format"]]]["mse_psnr"]
@@ -57,3 +57,34 @@ def test_photograph_against_reference_digest(built, name):
             assert q[k] == pytest.approx(v, rel=1e-12), k
         # exact integers vs the harness's rounded 0.21 / 0.72 / 0.07 products
         assert luma_mse(img, dec, w, h) == pytest.approx(q["mse_y"], rel=1e-10)
+
+
+HARNESS_FIELDS = ("image", "encoder", "format", "pixels", "time_us", "mps", "mse_r", "mse_g", "mse_b", "mse_max",
+                  "mse_rgb", "mse_y", "psnr_r", "psnr_g", "psnr_b", "psnr_min", "psnr_rgb", "psnr_y", "delta_min",
+                  "delta_rgb", "delta_y")
+
+
+@pytest.mark.skipif(not os.path.isdir(TEST_DATA), reason="reference test photographs not present")
+def test_tool_rows_match_the_harness_rows(built):
+    """The command-line tool's result rows (its RGB565 baseline, quality
+    record and formatting) equal the harness's printed rows field for field,
+    timings aside; the Goofy rows take the quality record of the reference's
+    blocks from the digests, which the GPU measurement must reproduce."""
+    from goofy_gb300 import tool
+
+    rows = {(r["encoder"], r["format"]): r for r in DIGESTS["harness_rows"]}
+    base_row = rows[("Baseline (Downsample x2)", "RGB565")]
+    name = base_row["image"]
+    img, w, h = g.read_png(os.path.join(TEST_DATA, name + ".png"))
+    base = tool.mse_psnr_images(img, tool.baseline_rgb565(img, w, h), w, h)
+    got = dict(zip(HARNESS_FIELDS, tool.result_row(name, "Baseline (Downsample x2)", "RGB565", w * h, 0, base,
+                                                   base).split(";")))
+    assert got == base_row
+    for fmt, cname in (("ETC1", "etc1s"), ("DXT1", "bc1")):
+        want = rows[("simd_goofy", fmt)]
+        q = DIGESTS["photos"][name][cname]["mse_psnr"]
+        got = dict(zip(HARNESS_FIELDS, tool.result_row(name, "simd_goofy", fmt, w * h, float(want["time_us"]), q,
+                                                       base).split(";")))
+        for k in HARNESS_FIELDS:
+            if k != "mps":  # the harness divides its rounded-to-print time; mps follows from time_us
+                assert got[k] == want[k], (fmt, k)
