@@ -65,6 +65,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world):
+    """The slowest rank's figure (a replica job ends when its last GPU ends);
+    CPU tensors over the gloo group, no data-path collective."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate_mpix_s(world, px_per_rank_step, steps, slowest_ms):
+    """Whole-job throughput: every rank's pixels over the slowest rank's time."""
+    return world * px_per_rank_step * steps / (slowest_ms / 1e3) / 1e6
+
+
 def read_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -515,13 +533,10 @@ def run_gpu(args):
     for k in range(args.steps):
         for c in codecs:
             per_launch[c].append(ev[k][c][0].elapsed_time(ev[k][c][1]))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world)
 
     px_per_step = 2 * W * H
-    value = world * px_per_step * args.steps / (total_ms / 1e3) / 1e6
+    value = job_rate_mpix_s(world, px_per_step, args.steps, total_ms)
 
     # e2e through the host C ABI from pinned memory
     e2e = None
@@ -545,12 +560,8 @@ def run_gpu(args):
                         rc = g.compress_host(c, out_ptr, in_ptr, W, H, 4 * W)
                         if rc != g.OK:
                             raise RuntimeError(g.last_error())
-                dt = time.perf_counter() - t0
-                if world > 1:
-                    t = torch.tensor([dt], dtype=torch.float64)
-                    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-                    dt = float(t.item())
-                return world * px_per_step * steps / dt / 1e6
+                dt = max_over_ranks(time.perf_counter() - t0, world)
+                return job_rate_mpix_s(world, px_per_step, steps, 1e3 * dt)
 
             value_e2e = e2e_rate(p_out, p_in, e2e_steps)
             g.set_host_path(g.HOST_PATH_STAGED)
@@ -620,7 +631,7 @@ def run_gpu(args):
     serving = None
     if not args.no_serving:
         serving = run_serving(args, g, local)
-    if not args.no_cpu:
+    if not args.no_cpu and rank == 0 and world == 1:
         from oracle import build as oracle_build
 
         oracle_build.build()
@@ -636,7 +647,8 @@ def run_gpu(args):
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
