@@ -489,7 +489,7 @@ def run_gpu(args):
     if args.sweep:
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         for c in codecs:
-            for threads, bpt, pers in [(t, b, p) for p in (0, 1) for t in (128, 256, 512) for b in (1, 2, 4)
+            for threads, bpt, pers in [(t, b, p) for p in (0, 1, 2) for t in (128, 256, 512) for b in (1, 2, 4)
                                        if not (p and b == 4)]:
                     g.set_tile(c, threads, bpt, pers)
                     ts = []

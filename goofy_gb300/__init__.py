@@ -136,6 +136,7 @@ def _declare(lib):
         "goofy_gpu_block_error_device": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
         "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
                                               ctypes.POINTER(ctypes.c_double), _VP]),
+        "goofy_gpu_pipeline_timeouts": (ctypes.c_int, [ctypes.POINTER(_U32), ctypes.c_int]),
         "goofy_gpu_mse_psnr": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, ctypes.POINTER(Quality)]),
         "goofy_gpu_png_info": (ctypes.c_int, [_VP, ctypes.c_size_t, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
         "goofy_gpu_png_decode": (ctypes.c_int, [_VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _U32, ctypes.c_int,
@@ -281,6 +282,15 @@ def get_tile(codec):
 def set_tile(codec, threads_per_cta, blocks_per_thread, persistent=0):
     t = Tile(threads_per_cta, blocks_per_thread, persistent)
     return lib().goofy_gpu_set_tile(codec, ctypes.byref(t))
+
+
+def pipeline_timeouts(reset=False):
+    """Bulk-copy pipeline waits that gave up on the current device (0 when healthy)."""
+    n = _U32()
+    rc = lib().goofy_gpu_pipeline_timeouts(ctypes.byref(n), 1 if reset else 0)
+    if rc != OK:
+        raise RuntimeError("pipeline_timeouts: %s %s" % (status_string(rc), last_error()))
+    return n.value
 
 
 def autotune(codec, dst, src, width, height, stride, reps=9):

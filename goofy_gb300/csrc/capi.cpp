@@ -55,7 +55,7 @@ using goofy_gpu::Tile;
 
 #define CUDA_TRY GOOFY_CUDA_TRY
 
-Tile g_tile[2] = {{256, 2, 0}, {256, 2, 0}};
+Tile g_tile[2] = {{128, 1, 0}, {512, 1, 2}};  // BC1: register-loading grid; ETC1s: bulk-copy pipeline
 std::mutex g_tile_mu;
 
 Tile tile_for(int codec)
@@ -216,9 +216,11 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
         const bool aligned = sa % 4 == 0 && stride % 4 == 0 && reinterpret_cast<uintptr_t>(ddst) % 8 == 0;
         if (dsrc && ddst && aligned) {
             const SrcAccess access = (sa % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
+            // bulk async copies only ever read device memory: host rows go through the register-loading kernel
+            Tile t = tile_for(codec);
+            if (t.persistent == 2) t.persistent = 0;
             CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(dsrc), stride,
-                                             static_cast<uint8_t*>(ddst), width, height, tile_for(codec), access,
-                                             hp.stream[0]));
+                                             static_cast<uint8_t*>(ddst), width, height, t, access, hp.stream[0]));
             CUDA_TRY(cudaStreamSynchronize(hp.stream[0]));
             return GOOFY_OK;
         }
@@ -432,7 +434,7 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
     for (int i = 0; i < 2 && result == GOOFY_OK; ++i)
         if (cudaEventCreate(&ev[i]) != cudaSuccess) result = cuda_fail(cudaGetLastError(), "cudaEventCreate");
     std::vector<Tile> candidates;
-    for (uint32_t persistent : {0u, 1u})
+    for (uint32_t persistent : {0u, 1u, 2u})
         for (uint32_t threads : {128u, 256u, 512u})
             for (uint32_t bpt : {1u, 2u, 4u})
                 if (goofy_gpu::tile_valid(Tile{threads, bpt, persistent}))
@@ -477,6 +479,15 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
         best->persistent = best_tile.persistent;
     }
     if (best_us) *best_us = best_time * 1e3f;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_pipeline_timeouts(uint32_t* count, int reset)
+{
+    if (!count) return GOOFY_ERR_INVALID;
+    unsigned int n = 0;
+    CUDA_TRY(goofy_gpu::pipeline_timeouts(&n, reset != 0));
+    *count = n;
     return GOOFY_OK;
 }
 

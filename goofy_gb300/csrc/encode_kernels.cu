@@ -178,6 +178,10 @@ cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* 
     if (!tile_valid(tile)) return cudaErrorInvalidValue;
     const uint32_t bw = width / 4, bh = height / 4;
     if (bw == 0 || bh == 0) return cudaSuccess;
+    if (tile.persistent == 2) {
+        if (access == SrcAccess::kVec16) return launch_image_tma(codec, src, stride, dst, width, height, tile, stream);
+        tile.persistent = 0;  // word-aligned rows: the register-loading kernel with the same shape
+    }
     if (codec == kBC1) return launch_access<kBC1>(src, stride, dst, bw, bh, tile, access, stream);
     return launch_access<kETC1S>(src, stride, dst, bw, bh, tile, access, stream);
 }

@@ -1,0 +1,210 @@
+// encode_tma.cu -- the image encoder fed by bulk asynchronous copies.
+//
+// A resident grid of CTAs, each with one producer warp and C compute warps
+// (C = threads / 32).  Work is cut into tiles of 4 pixel rows x (32 * C * BPT)
+// blocks; CTA b takes tiles b, b + grid, ...  The producer's elected lane
+// copies each tile's four row segments (16 bytes per block, contiguous in the
+// source) into the next free stage of a shared-memory ring with
+// cp.async.bulk, counted on that stage's "full" mbarrier; compute warps wait
+// for it, pull their blocks into registers with conflict-free 128-bit shared
+// loads (lane l of a warp reads 16 contiguous bytes, the warp 512), release
+// the stage on its "empty" mbarrier and run the same block codec as every
+// other kernel, storing 8 bytes per block with streaming stores.  Loads never
+// sit in the compute warps' registers, so the integer math of one tile
+// overlaps the HBM reads of the next stages.
+//
+// Needs 16-byte aligned source rows (base and stride); other images take the
+// register-loading kernels.  Every wait is bounded (async_copy.cuh): a stuck
+// barrier ends the kernel with a counted time-out instead of a hang, and the
+// producer then waits (bounded) for the copies it issued before its CTA exits.
+#include <cuda_runtime.h>
+
+#include "async_copy.cuh"
+#include "block_codec.cuh"
+#include "device_io.cuh"
+#include "kernels.h"
+
+namespace goofy_gpu {
+
+__device__ unsigned int g_pipeline_timeouts;
+
+struct TmaLayout {
+    uint32_t tile_blocks, row_bytes, stage_bytes, stages;
+};
+
+__host__ __device__ inline TmaLayout tma_layout(uint32_t compute_threads, uint32_t bpt)
+{
+    TmaLayout l;
+    l.tile_blocks = compute_threads * bpt;
+    l.row_bytes = 16u * l.tile_blocks;
+    l.stage_bytes = 4u * l.row_bytes;
+    const uint32_t s = 65536u / l.stage_bytes;  // about 64 KB of ring per CTA
+    l.stages = s < 2u ? 2u : s > 6u ? 6u : s;
+    return l;
+}
+
+inline size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * (l.stage_bytes + 16u) + 128u; }
+
+template <int CODEC, int BPT>
+__global__ void __launch_bounds__(544) encode_image_tma(const uint8_t* __restrict__ src, size_t stride,
+                                                        uint8_t* __restrict__ dst, uint32_t bw, uint32_t tiles_per_row,
+                                                        uint32_t total_tiles, uint32_t tile_magic)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ uint32_t abort_flag;
+    const uint32_t compute_warps = (blockDim.x >> 5) - 1u;
+    const TmaLayout L = tma_layout(compute_warps * 32u, BPT);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.stages * L.stage_bytes);
+    uint64_t* empty = full + L.stages;
+    uint8_t* ctrl_lut = reinterpret_cast<uint8_t*>(empty + L.stages);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < L.stages; ++s) {
+            mbar_init(&full[s], 1u);
+            mbar_init(&empty[s], compute_warps);
+        }
+        abort_flag = 0u;
+        mbar_init_fence();
+    }
+    if constexpr (CODEC == kETC1S) fill_ctrl_lut(ctrl_lut);
+    __syncthreads();
+
+    if (warp == compute_warps) {  // producer
+        if (lane != 0) return;
+        uint32_t issued = 0, slot = 0, phase = 0;
+        for (uint32_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+            if (issued >= L.stages && !mbar_wait(&empty[slot], phase ^ 1u, &abort_flag, &g_pipeline_timeouts))
+                break;
+            uint32_t tx;
+            const uint32_t by = div_magic(t, tiles_per_row, tile_magic, tx);
+            const uint32_t bx0 = tx * L.tile_blocks;
+            const uint32_t nb = min(L.tile_blocks, bw - bx0);
+            const uint32_t bytes = 16u * nb;
+            mbar_arrive_expect_tx(&full[slot], 4u * bytes);
+            const uint8_t* row = src + (size_t)by * 4u * stride + 16u * (size_t)bx0;
+            uint8_t* buf = smem + slot * L.stage_bytes;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) bulk_copy_g2s(buf + r * L.row_bytes, row + r * stride, bytes, &full[slot]);
+            ++issued;
+            if (++slot == L.stages) {
+                slot = 0;
+                phase ^= 1u;
+            }
+        }
+        if (*static_cast<volatile uint32_t*>(&abort_flag)) {
+            // the copies of the last stages may still be landing: wait for them (bounded) before exiting
+            const uint32_t n = issued < L.stages ? issued : L.stages;
+            for (uint32_t i = issued - n; i < issued; ++i)
+                mbar_wait(&full[i % L.stages], (i / L.stages) & 1u, nullptr, &g_pipeline_timeouts);
+        }
+        return;
+    }
+
+    uint32_t slot = 0, phase = 0;
+    for (uint32_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+        if (!mbar_wait(&full[slot], phase, &abort_flag, &g_pipeline_timeouts)) break;
+        uint32_t tx;
+        const uint32_t by = div_magic(t, tiles_per_row, tile_magic, tx);
+        const uint32_t bx0 = tx * L.tile_blocks;
+        const uint32_t nb = min(L.tile_blocks, bw - bx0);
+        const uint8_t* buf = smem + slot * L.stage_bytes;
+        uint32_t w[BPT][16];
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+            const uint32_t b = (warp * BPT + j) * 32u + lane;
+            if (b < nb) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(buf + r * L.row_bytes + 16u * b);
+                    w[j][4 * r + 0] = v.x;
+                    w[j][4 * r + 1] = v.y;
+                    w[j][4 * r + 2] = v.z;
+                    w[j][4 * r + 3] = v.w;
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+        uint8_t* out = dst + ((size_t)by * bw + bx0) * 8u;
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+            const uint32_t b = (warp * BPT + j) * 32u + lane;
+            if (b < nb) st_stream8(out + 8u * (size_t)b, encode_block<CODEC>(w[j], ctrl_lut));
+        }
+        if (++slot == L.stages) {
+            slot = 0;
+            phase ^= 1u;
+        }
+    }
+}
+
+namespace {
+
+template <int CODEC, int BPT>
+cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh, uint32_t threads,
+                         cudaStream_t stream)
+{
+    const TmaLayout L = tma_layout(threads, BPT);
+    const size_t smem = tma_smem_bytes(L);
+    const uint32_t block = threads + 32u;
+    // per device: dynamic shared memory opt-in and resident CTAs per SM, by block size
+    static int resident[64][3] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const int slot = threads == 128 ? 0 : threads == 256 ? 1 : 2;
+    if (resident[dev][slot] == 0) {
+        // the opt-in covers the largest ring of any block size of this instantiation
+        size_t most = 0;
+        for (uint32_t t : {128u, 256u, 512u}) {
+            const size_t b = tma_smem_bytes(tma_layout(t, BPT));
+            most = b > most ? b : most;
+        }
+        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+        if (e != cudaSuccess) return e;
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_tma<CODEC, BPT>, (int)block, smem);
+        if (e != cudaSuccess) return e;
+        resident[dev][slot] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }
+    const uint32_t tiles_per_row = (bw + L.tile_blocks - 1) / L.tile_blocks;
+    const uint64_t total = (uint64_t)tiles_per_row * bh;
+    if (total > 0x7fffffffull) return cudaErrorInvalidValue;
+    const uint32_t grid = (uint32_t)(total < (uint64_t)resident[dev][slot] ? total : resident[dev][slot]);
+    encode_image_tma<CODEC, BPT><<<grid, block, smem, stream>>>(src, stride, dst, bw, tiles_per_row, (uint32_t)total,
+                                                               0xffffffffu / tiles_per_row);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
+                             uint32_t height, Tile tile, cudaStream_t stream)
+{
+    const uint32_t bw = width / 4, bh = height / 4;
+    if (bw == 0 || bh == 0) return cudaSuccess;
+    if (reinterpret_cast<uintptr_t>(src) % 16 || stride % 16) return cudaErrorInvalidValue;
+    if (codec == kBC1) {
+        if (tile.bpt == 1) return launch_tma_t<kBC1, 1>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_t<kBC1, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+    } else {
+        if (tile.bpt == 1) return launch_tma_t<kETC1S, 1>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_t<kETC1S, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t pipeline_timeouts(unsigned int* count, bool reset)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(count, g_pipeline_timeouts, sizeof(unsigned int));
+    if (e == cudaSuccess && reset) {
+        const unsigned int zero = 0;
+        e = cudaMemcpyToSymbol(g_pipeline_timeouts, &zero, sizeof(unsigned int));
+    }
+    return e;
+}
+
+}  // namespace goofy_gpu

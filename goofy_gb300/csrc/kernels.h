@@ -11,13 +11,14 @@ namespace goofy_gpu {
 struct Tile {
     uint32_t threads;     // threads per CTA: 128, 256 or 512
     uint32_t bpt;         // 4x4 blocks per thread and segment: 1, 2 or 4 (1 or 2 when persistent)
-    uint32_t persistent;  // 0: one segment per warp; 1: resident grid looping over segments with prefetch
+    uint32_t persistent;  // 0: one segment per warp; 1: resident grid looping over segments with prefetch;
+                          // 2: resident grid fed by bulk copies into a shared-memory ring (+1 producer warp)
 };
 
 inline bool tile_valid(const Tile& t)
 {
     if (t.threads != 128 && t.threads != 256 && t.threads != 512) return false;
-    if (t.persistent > 1) return false;
+    if (t.persistent > 2) return false;
     return t.bpt == 1 || t.bpt == 2 || (t.bpt == 4 && !t.persistent);
 }
 
@@ -31,5 +32,13 @@ enum class SrcAccess : int {
 // blocks at `dst`.  Only enqueues; returns the launch error, if any.
 cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
                          uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream);
+
+// The bulk-copy pipeline kernel (tile.persistent == 2); needs a 16-byte
+// aligned source base and stride.
+cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
+                             uint32_t height, Tile tile, cudaStream_t stream);
+
+// Pipeline waits that gave up on the current device since the last reset.
+cudaError_t pipeline_timeouts(unsigned int* count, bool reset);
 
 }  // namespace goofy_gpu

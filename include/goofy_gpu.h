@@ -107,7 +107,10 @@ void goofy_gpu_host_free(void* p);
 typedef struct goofy_gpu_tile {
     uint32_t threads_per_cta;   /* 128, 256, 512 */
     uint32_t blocks_per_thread; /* 4x4 blocks a thread encodes per segment: 1, 2, 4 (1, 2 if persistent) */
-    uint32_t persistent;        /* 0: one segment per warp; 1: resident grid, loop with prefetch */
+    uint32_t persistent;        /* 0: one segment per warp; 1: resident grid, loop with prefetch;
+                                 * 2: resident grid, one producer warp streams tiles into a
+                                 *    shared-memory ring with bulk async copies (1, 2 blocks per
+                                 *    thread; 16-byte aligned sources, others run shape 0) */
 } goofy_gpu_tile;
 
 /* Get / set the tile the image kernels launch with, per codec. */
@@ -121,6 +124,11 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
  * median launch time in microseconds.  Synchronous.  No reference counterpart. */
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
+
+/* Waits of the bulk-copy pipeline (tile mode 2) that gave up after their
+ * time limit on the current device (each ends its kernel early instead of
+ * hanging); `reset` != 0 zeroes the count.  0 in a healthy run.  Synchronous. */
+int goofy_gpu_pipeline_timeouts(uint32_t* count, int reset);
 
 /* ---- decoding and encode quality -------------------------------------------- */
 

@@ -73,7 +73,9 @@ def test_tile_get_set(built):
         assert g.get_tile(codec) == (512, 2, 1)
         assert g.set_tile(codec, 256, 4, 0) == g.OK
         assert g.set_tile(codec, 256, 4, 1) == g.ERR_INVALID
-        assert g.set_tile(codec, 256, 2, 2) == g.ERR_INVALID
+        assert g.set_tile(codec, 256, 2, 2) == g.OK
+        assert g.set_tile(codec, 256, 4, 2) == g.ERR_INVALID
+        assert g.set_tile(codec, 256, 2, 3) == g.ERR_INVALID
         assert g.set_tile(codec, 96, 2) == g.ERR_INVALID
         assert g.set_tile(codec, 256, 3) == g.ERR_INVALID
         assert g.set_tile(codec, *before) == g.OK

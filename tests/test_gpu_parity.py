@@ -15,7 +15,7 @@ from goofy_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 CODECS = [("bc1", g.CODEC_BC1), ("etc1s", g.CODEC_ETC1S)]
-TILES = [(t, b, p) for p in (0, 1) for t in (128, 256, 512) for b in (1, 2, 4) if not (p and b == 4)]
+TILES = [(t, b, p) for p in (0, 1, 2) for t in (128, 256, 512) for b in (1, 2, 4) if not (p and b == 4)]
 GUARD = 256
 
 
@@ -64,7 +64,7 @@ def test_ragged_sizes(cuda, name, codec, w, h):
     rng = np.random.default_rng(w * 1000 + h)
     img = rng.integers(0, 256, (h, 4 * w), dtype=np.uint8)
     want = oracle.encode(codec, img, w, h)
-    for tile in ((256, 1, 0), (128, 4, 0), (256, 2, 1)):
+    for tile in ((256, 1, 0), (128, 4, 0), (256, 2, 1), (128, 1, 2), (512, 2, 2)):
         np.testing.assert_array_equal(device_encode(cuda, codec, img, w, h, tile=tile), want)
 
 
@@ -132,13 +132,20 @@ def test_full_size_scene_8192(cuda, name, codec):
     want = oracle.encode(codec, img, w, h, threads=0)
     src = cuda.from_numpy(img.reshape(-1)).cuda()
     dst = cuda.empty(g.out_size(w, h), dtype=cuda.uint8, device="cuda")
-    for _ in range(2):
-        dst.fill_(0)
-        assert g.compress_device(codec, dst.data_ptr(), src.data_ptr(), w, h, 4 * w,
-                                 cuda.cuda.current_stream().cuda_stream) == g.OK
-        cuda.cuda.synchronize()
-        got = dst.cpu().numpy()
-        assert hashlib.sha256(got.tobytes()).hexdigest() == hashlib.sha256(want.tobytes()).hexdigest()
+    before = g.get_tile(codec)
+    try:
+        for tile in (before, (256, 1, 2), (512, 2, 2), (128, 2, 2)):
+            assert g.set_tile(codec, *tile) == g.OK
+            for _ in range(2):
+                dst.fill_(0)
+                assert g.compress_device(codec, dst.data_ptr(), src.data_ptr(), w, h, 4 * w,
+                                         cuda.cuda.current_stream().cuda_stream) == g.OK
+                cuda.cuda.synchronize()
+                got = dst.cpu().numpy()
+                assert hashlib.sha256(got.tobytes()).hexdigest() == hashlib.sha256(want.tobytes()).hexdigest(), tile
+    finally:
+        g.set_tile(codec, *before)
+    assert g.pipeline_timeouts() == 0
 
 
 @pytest.mark.parametrize("name,codec", CODECS)
@@ -153,3 +160,14 @@ def test_full_size_stress_4096(cuda, name, codec):
     for k in range(4):
         part = device_encode(cuda, codec, np.ascontiguousarray(img[:, 4 * k * q:4 * (k + 1) * q]), q, h)
         np.testing.assert_array_equal(part.reshape(h // 4, q // 4, 8), full[:, k * q // 4:(k + 1) * q // 4])
+
+
+def test_pipeline_reports_no_timeouts(cuda):
+    """The bulk-copy pipeline's bounded waits never expire in a healthy run."""
+    g.pipeline_timeouts(reset=True)
+    img = workloads.scene(1024, 512, 3)
+    for codec in (0, 1):
+        for tile in ((128, 1, 2), (256, 2, 2), (512, 1, 2)):
+            np.testing.assert_array_equal(device_encode(cuda, codec, img, 1024, 512, tile=tile),
+                                          oracle.encode(codec, img, 1024, 512))
+    assert g.pipeline_timeouts() == 0
