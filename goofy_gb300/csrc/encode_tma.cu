@@ -38,7 +38,9 @@ __host__ __device__ inline TmaLayout tma_layout(uint32_t compute_threads, uint32
     l.tile_blocks = compute_threads * bpt;
     l.row_bytes = 16u * l.tile_blocks;
     l.stage_bytes = 4u * l.row_bytes;
-    const uint32_t s = 65536u / l.stage_bytes;  // about 64 KB of ring per CTA
+    // ring budget scaled with the CTA (112 KB at 512 compute threads), so the
+    // CTAs the registers allow per SM also fit in shared memory
+    const uint32_t s = (114688u / 512u * compute_threads) / l.stage_bytes;
     l.stages = s < 2u ? 2u : s > 6u ? 6u : s;
     return l;
 }
