@@ -63,18 +63,24 @@ GOOFY_FN uint32_t luma(uint32_t px) { return luma_sum(px, 3u) >> 2; }
 // to5 on both 16-bit lanes
 GOOFY_FN uint32_t to5x2(uint32_t lanes) { return ((vmax2(lanes, 0x00010001u) - 0x00010001u) >> 3) & 0x001f001fu; }
 
+// Lane-wise min / max of N words as a tree of three-input steps, min(min(a, b), c),
+// which the compiler issues as single three-input lane min / max instructions.
 template <int N>
 GOOFY_FN uint32_t tree_min(const uint32_t* v)
 {
     if constexpr (N == 1) return v[0];
-    else return vmin2(tree_min<N / 2>(v), tree_min<N / 2>(v + N / 2));
+    else if constexpr (N == 2) return vmin2(v[0], v[1]);
+    else if constexpr (N == 3) return vmin2(vmin2(v[0], v[1]), v[2]);
+    else return vmin2(vmin2(tree_min<N / 3>(v), tree_min<N / 3>(v + N / 3)), tree_min<N - 2 * (N / 3)>(v + 2 * (N / 3)));
 }
 
 template <int N>
 GOOFY_FN uint32_t tree_max(const uint32_t* v)
 {
     if constexpr (N == 1) return v[0];
-    else return vmax2(tree_max<N / 2>(v), tree_max<N / 2>(v + N / 2));
+    else if constexpr (N == 2) return vmax2(v[0], v[1]);
+    else if constexpr (N == 3) return vmax2(vmax2(v[0], v[1]), v[2]);
+    else return vmax2(vmax2(tree_max<N / 3>(v), tree_max<N / 3>(v + N / 3)), tree_max<N - 2 * (N / 3)>(v + 2 * (N / 3)));
 }
 
 // Run starts of etc1BrighnessRangeTocontrolByte (goofy_tc.h:1040-1057); all

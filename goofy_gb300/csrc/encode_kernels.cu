@@ -128,10 +128,27 @@ static int resident_ctas(uint32_t threads)
     return cached[slot];
 }
 
+// The image kernels run with the shared-memory-heavy carveout of the
+// bulk-copy kernel (their loads bypass L1 anyway), so alternating the two
+// does not reconfigure the SMs between launches.
+template <typename K>
+static void prefer_shared(K kernel, int slot)
+{
+    static bool done[64][2] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev][slot]) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+        cudaSuccess)
+        cudaGetLastError();
+    done[dev][slot] = true;
+}
+
 template <int CODEC, int BPT, SrcAccess ACCESS>
 static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
                             uint32_t threads, bool persistent, cudaStream_t stream)
 {
+    prefer_shared(encode_image_kernel<CODEC, BPT, ACCESS>, 0);
+    if constexpr (BPT <= 2) prefer_shared(encode_image_persistent<CODEC, BPT, ACCESS>, 1);
     const uint32_t segs = (bw + 32u * BPT - 1) / (32u * BPT);
     const uint64_t total = (uint64_t)segs * bh;
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;

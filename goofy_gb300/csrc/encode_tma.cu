@@ -166,6 +166,9 @@ cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32
         }
         e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
         int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_tma<CODEC, BPT>, (int)block, smem);
