@@ -598,10 +598,11 @@ def run_gpu(args):
     dom = max(codecs, key=lambda c: statistics.mean(per_launch[c]))
     dom_ms = statistics.mean(per_launch[dom])
     achieved = ALG_BYTES_PER_PX * W * H / (dom_ms / 1e3) / 1e9
-    traffic = read_traffic("encode_image_" + names[dom] + "_8192")
+    kernel = "encode_image_tma" if g.get_tile(dom)[2] == 2 else "encode_image_kernel"
+    traffic = read_traffic("%s_%s_8192" % (kernel, names[dom]))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "encode_image_kernel<" +
-                names[dom] + ">", "algorithmic_bytes_per_launch": int(ALG_BYTES_PER_PX * W * H),
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "%s<%s>" % (kernel, names[dom]),
+                "algorithmic_bytes_per_launch": int(ALG_BYTES_PER_PX * W * H),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s"}
     cpu = None
