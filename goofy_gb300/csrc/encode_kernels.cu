@@ -14,6 +14,8 @@
 // roofline.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "block_codec.cuh"
 #include "device_io.cuh"
 #include "kernels.h"
@@ -115,17 +117,20 @@ __global__ void __launch_bounds__(512) encode_image_persistent(const uint8_t* __
 template <int CODEC, int BPT, SrcAccess ACCESS>
 static int resident_ctas(uint32_t threads)
 {
-    // cached per instantiation and block size (the device is the current one)
-    static int cached[3] = {0, 0, 0};
+    // cached per instantiation, device and block size
+    static std::atomic<int> cached[64][3];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
     const int slot = threads == 128 ? 0 : threads == 256 ? 1 : 2;
-    if (cached[slot] == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
+    int n = cached[dev][slot].load(std::memory_order_relaxed);
+    if (n == 0) {
+        int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_persistent<CODEC, BPT, ACCESS>, threads, 0);
-        cached[slot] = sms * (per_sm > 0 ? per_sm : 1);
+        n = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        cached[dev][slot].store(n, std::memory_order_relaxed);
     }
-    return cached[slot];
+    return n;
 }
 
 // The image kernels run with the shared-memory-heavy carveout of the
@@ -134,13 +139,14 @@ static int resident_ctas(uint32_t threads)
 template <typename K>
 static void prefer_shared(K kernel, int slot)
 {
-    static bool done[64][2] = {};
+    static std::atomic<bool> done[64][2];
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev][slot]) return;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev][slot].load(std::memory_order_relaxed))
+        return;
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
         cudaSuccess)
         cudaGetLastError();
-    done[dev][slot] = true;
+    done[dev][slot].store(true, std::memory_order_relaxed);
 }
 
 template <int CODEC, int BPT, SrcAccess ACCESS>

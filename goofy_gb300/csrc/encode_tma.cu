@@ -19,6 +19,8 @@
 // producer then waits (bounded) for the copies it issued before its CTA exits.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "async_copy.cuh"
 #include "block_codec.cuh"
 #include "device_io.cuh"
@@ -151,13 +153,14 @@ cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32
     const size_t smem = tma_smem_bytes(L);
     const uint32_t block = threads + 32u;
     // per device: dynamic shared memory opt-in and resident CTAs per SM, by block size
-    static int resident[64][3] = {};
+    static std::atomic<int> resident[64][3];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const int slot = threads == 128 ? 0 : threads == 256 ? 1 : 2;
-    if (resident[dev][slot] == 0) {
+    int ctas = resident[dev][slot].load(std::memory_order_relaxed);
+    if (ctas == 0) {
         // the opt-in covers the largest ring of any block size of this instantiation
         size_t most = 0;
         for (uint32_t t : {128u, 256u, 512u}) {
@@ -173,12 +176,13 @@ cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_tma<CODEC, BPT>, (int)block, smem);
         if (e != cudaSuccess) return e;
-        resident[dev][slot] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        ctas = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        resident[dev][slot].store(ctas, std::memory_order_relaxed);
     }
     const uint32_t tiles_per_row = (bw + L.tile_blocks - 1) / L.tile_blocks;
     const uint64_t total = (uint64_t)tiles_per_row * bh;
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;
-    const uint32_t grid = (uint32_t)(total < (uint64_t)resident[dev][slot] ? total : resident[dev][slot]);
+    const uint32_t grid = (uint32_t)(total < (uint64_t)ctas ? total : (uint64_t)ctas);
     encode_image_tma<CODEC, BPT><<<grid, block, smem, stream>>>(src, stride, dst, bw, tiles_per_row, (uint32_t)total,
                                                                0xffffffffu / tiles_per_row);
     return cudaGetLastError();
