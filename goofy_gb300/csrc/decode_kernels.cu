@@ -14,118 +14,11 @@
 #include <cuda_runtime.h>
 
 #include "block_codec.cuh"
+#include "block_decode.cuh"
 #include "decode.h"
 #include "device_io.cuh"
 
 namespace goofy_gpu {
-
-// 5/6-bit endpoint channel to 8 bits: (c << 3) | (c >> 2), (c << 2) | (c >> 4).
-__device__ __forceinline__ uint32_t expand565(uint32_t v)
-{
-    const uint32_t r = (v >> 11) & 31u, g = (v >> 5) & 63u, b = v & 31u;
-    return (r << 3 | r >> 2) | (g << 2 | g >> 4) << 8 | (b << 3 | b >> 2) << 16 | 0xff000000u;
-}
-
-__device__ __forceinline__ uint32_t chan(uint32_t w, int c) { return (w >> (8 * c)) & 0xffu; }
-
-// Palette of a BC1 block as four RGBA words.
-__device__ __forceinline__ void bc1_palette(uint32_t ends, uint32_t (&pal)[4])
-{
-    const uint32_t a = ends & 0xffffu, b = ends >> 16;
-    pal[0] = expand565(a);
-    pal[1] = expand565(b);
-    uint32_t p2 = 0, p3 = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const uint32_t p = chan(pal[0], c), q = chan(pal[1], c);
-        if (a > b) {
-            p2 |= ((2 * p + q) / 3) << (8 * c);
-            p3 |= ((p + 2 * q) / 3) << (8 * c);
-        } else {
-            p2 |= ((p + q) / 2) << (8 * c);
-        }
-    }
-    pal[2] = p2 | 0xff000000u;
-    pal[3] = a > b ? (p3 | 0xff000000u) : 0u;  // 3-colour mode: transparent black
-}
-
-// The 4 colours of one ETC1 sub-block: clamp(base + modifier) per channel.
-__device__ __forceinline__ void etc1_subpalette(uint32_t base, uint32_t table, uint32_t (&pal)[4])
-{
-    const int small = table == 0 ? 2 : table == 1 ? 5 : table == 2 ? 9 : table == 3 ? 13
-                    : table == 4 ? 18 : table == 5 ? 24 : table == 6 ? 33 : 47;
-    const int large = table == 0 ? 8 : table == 1 ? 17 : table == 2 ? 29 : table == 3 ? 42
-                    : table == 4 ? 60 : table == 5 ? 80 : table == 6 ? 106 : 183;
-    const int mod[4] = {small, large, -small, -large};  // pixel index value 0..3
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        uint32_t w = 0xff000000u;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const int v = (int)chan(base, c) + mod[k];
-            w |= (uint32_t)min(max(v, 0), 255) << (8 * c);
-        }
-        pal[k] = w;
-    }
-}
-
-// Decode one block into 16 row-major RGBA words.  Returns false for an ETC1
-// differential block whose second colour leaves 0..31 (an ETC2 mode).
-template <int CODEC>
-__device__ __forceinline__ bool decode_block(uint2 blk, uint32_t (&px)[16])
-{
-    if constexpr (CODEC == kBC1) {
-        uint32_t pal[4];
-        bc1_palette(blk.x, pal);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const uint32_t idx = (blk.y >> (2 * i)) & 3u;
-            px[i] = idx == 0 ? pal[0] : idx == 1 ? pal[1] : idx == 2 ? pal[2] : pal[3];
-        }
-        return true;
-    } else {
-        // the block is big-endian: bytes 0..3 of blk.x are bits 63..32
-        const uint32_t w0 = __byte_perm(blk.x, 0, 0x0123), w1 = __byte_perm(blk.y, 0, 0x0123);
-        const bool diff = (w0 >> 1) & 1u, flip = w0 & 1u;
-        uint32_t base[2] = {0, 0};
-        bool ok = true;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            uint32_t b0, b1;
-            if (diff) {
-                const int c5 = (int)(w0 >> (27 - 8 * c)) & 31;
-                int d = (int)(w0 >> (24 - 8 * c)) & 7;
-                d = d >= 4 ? d - 8 : d;
-                const int c52 = c5 + d;
-                ok = ok && c52 >= 0 && c52 <= 31;
-                const int c5b = min(max(c52, 0), 31);
-                b0 = (uint32_t)(c5 << 3 | c5 >> 2);
-                b1 = (uint32_t)(c5b << 3 | c5b >> 2);
-            } else {
-                const uint32_t a = (w0 >> (28 - 8 * c)) & 15u, b = (w0 >> (24 - 8 * c)) & 15u;
-                b0 = a << 4 | a;
-                b1 = b << 4 | b;
-            }
-            base[0] |= b0 << (8 * c);
-            base[1] |= b1 << (8 * c);
-        }
-        uint32_t pal0[4], pal1[4];
-        etc1_subpalette(base[0], (w0 >> 5) & 7u, pal0);
-        etc1_subpalette(base[1], (w0 >> 2) & 7u, pal1);
-#pragma unroll
-        for (int y = 0; y < 4; ++y)
-#pragma unroll
-            for (int x = 0; x < 4; ++x) {
-                const int k = 4 * x + y;
-                const uint32_t idx = ((w1 >> (16 + k)) & 1u) << 1 | ((w1 >> k) & 1u);
-                const bool sub = flip ? (y >= 2) : (x >= 2);
-                const uint32_t a = idx == 0 ? pal0[0] : idx == 1 ? pal0[1] : idx == 2 ? pal0[2] : pal0[3];
-                const uint32_t b = idx == 0 ? pal1[0] : idx == 1 ? pal1[1] : idx == 2 ? pal1[2] : pal1[3];
-                px[4 * y + x] = ok ? (sub ? b : a) : 0u;
-            }
-        return ok;
-    }
-}
 
 __device__ __forceinline__ uint2 load_block8(const uint8_t* p)
 {
@@ -139,12 +32,13 @@ __global__ void __launch_bounds__(256) decode_image_kernel(const uint8_t* __rest
                                                            uint32_t nblk, uint8_t* __restrict__ rgba, size_t stride,
                                                            unsigned long long* __restrict__ unsupported)
 {
+    __shared__ uint32_t pal[8 * 256];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool ok = true;
     if (i < nblk) {
         const uint32_t by = i / bw, bx = i - by * bw;
         uint32_t px[16];
-        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
+        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), pal + threadIdx.x, blockDim.x, px);
         uint8_t* row = rgba + (size_t)by * 4u * stride + 16u * (size_t)bx;
 #pragma unroll
         for (int y = 0; y < 4; ++y)
@@ -196,11 +90,14 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
                                                           size_t stride, bool vec16,
                                                           unsigned long long* __restrict__ sums)
 {
+    __shared__ uint32_t pal[8 * 256];
     unsigned long long s[6] = {0, 0, 0, 0, 0, 0};
+    const uint32_t bw_magic = 0xffffffffu / bw;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
-        const uint32_t by = i / bw, bx = i - by * bw;
+        uint32_t bx;
+        const uint32_t by = div_magic(i, bw, bw_magic, bx);
         uint32_t px[16], w[16];
-        const bool ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), px);
+        const bool ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), pal + threadIdx.x, blockDim.x, px);
         load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
         uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
 #pragma unroll

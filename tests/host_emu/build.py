@@ -8,7 +8,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 SO = os.path.join(HERE, "_build", "libblock_codec_host.so")
 SOURCES = [os.path.join(HERE, "block_codec_host.cpp"), os.path.join(HERE, "host_emulation.h"),
-           os.path.join(ROOT, "goofy_gb300", "csrc", "block_codec.cuh")]
+           os.path.join(ROOT, "goofy_gb300", "csrc", "block_codec.cuh"),
+           os.path.join(ROOT, "goofy_gb300", "csrc", "block_decode.cuh")]
 
 
 def load():
@@ -19,5 +20,8 @@ def load():
     lib = ctypes.CDLL(SO)
     lib.host_emu_encode.restype = ctypes.c_int
     lib.host_emu_encode.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint,
+                                    ctypes.c_uint]
+    lib.host_emu_decode.restype = ctypes.c_long
+    lib.host_emu_decode.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p,
                                     ctypes.c_uint]
     return lib
