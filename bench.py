@@ -209,6 +209,37 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
 
 
+def run_mips(g, torch, workloads, img, d_src, stream):
+    """Device mip chain of the 8192x8192 image (levels 4096x4096 .. 4x4; up to
+    6 levels per launch): median time, HBM rate for the algorithmic bytes (the
+    image read once, every level written once) and equality with the host
+    chain."""
+    nbytes = g.lib().goofy_gpu_mip_arena_bytes(W, H)
+    arena = torch.empty(nbytes + 256, dtype=torch.uint8, device=d_src.device)
+    base = arena.data_ptr() + (-arena.data_ptr()) % 256
+    sh = stream.cuda_stream
+    ts = []
+    for _ in range(10):
+        e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_a.record(stream)
+        levels = g.generate_mips(d_src, W, H, 4 * W, base, nbytes, sh)
+        e_b.record(stream)
+        e_b.synchronize()
+        ts.append(e_a.elapsed_time(e_b))
+    ms = statistics.median(ts[3:])
+    moved = 4 * W * H + sum(4 * lw * lh for (_, lw, lh, _) in levels[1:])  # read the image once, write every level
+    host = arena.cpu().numpy()
+    off0 = base - arena.data_ptr()
+    exact, cur, cw, ch = True, img, W, H
+    for (ptr, lw, lh, pitch) in levels[1:]:
+        cur, cw, ch = workloads.downsample(cur, cw, ch)
+        o = off0 + (ptr - base)
+        exact = exact and bool((host[o:o + pitch * lh].reshape(lh, pitch)[:, :4 * lw] == cur).all())
+    return {"workload": "mip chain of the 8192x8192 scene, levels 4096x4096 .. 4x4 (2x2 box with rounding)",
+            "levels": len(levels) - 1, "us": round(ms * 1e3, 2),
+            "bytes_moved": moved, "hbm_gbs": round(moved / (ms / 1e3) / 1e9, 1), "bit_exact_vs_host_chain": exact}
+
+
 def run_batched(args, g, torch, stream, dev):
     """Mixed batch: `--batch-textures` textures (64..2048 per side, 20% with
     mip chains, BC1 / ETC1s 50/50), every level resident in HBM.  Batched =
@@ -626,6 +657,7 @@ def run_gpu(args):
         quality[names[c]] = {"psnr_rgb_db": round(psnr, 5), "unsupported_blocks": int(sums[4]),
                              "decode_error_kernel_us": round(ms * 1e3, 2),
                              "decode_error_hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
+    mips = run_mips(g, torch, workloads, img, src[0], stream)
     batched = None
     if not args.no_batched:
         batched = run_batched(args, g, torch, stream, dev)
@@ -644,7 +676,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}

@@ -6,9 +6,10 @@
 // level is produced from the one above by a 2x2 box filter with rounding,
 // (a + b + c + d + 2) >> 2 per channel, an axis that is already 4 pixels
 // being copied instead of halved -- the rule of the workload generator's
-// goofy_synth_downsample, so device and host chains are bit-identical.  One
-// launch per level (each level depends on the previous one); a thread makes
-// one output pixel, channel pairs summed in 16-bit lanes.
+// goofy_synth_downsample, so device and host chains are bit-identical.  While
+// both axes halve, one launch makes up to 6 levels from shared-memory tiles
+// (mip_fused_kernel); the rest take one launch per level, a thread per output
+// pixel.  Channel pairs are summed in 16-bit lanes.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -26,6 +27,10 @@ __device__ __forceinline__ uint32_t box4(uint32_t a, uint32_t b, uint32_t c, uin
     return ((rb >> 2) & m) | (((ga >> 2) & m) << 8);
 }
 
+// One output pixel per thread.  FX = 2 (the level halves horizontally) with
+// 8-byte aligned rows reads the two source pixels of each row with one 8-byte
+// load; otherwise four 4-byte loads.
+template <bool PAIR>
 __global__ void __launch_bounds__(256) mip_level_kernel(const uint8_t* __restrict__ src, size_t src_stride,
                                                         uint8_t* __restrict__ dst, size_t dst_stride, uint32_t dw,
                                                         uint32_t dh, uint32_t fx, uint32_t fy)
@@ -34,14 +39,96 @@ __global__ void __launch_bounds__(256) mip_level_kernel(const uint8_t* __restric
     if (x >= dw || y >= dh) return;
     const uint8_t* r0 = src + (size_t)(y * fy) * src_stride + 4u * (size_t)(x * fx);
     const uint8_t* r1 = r0 + src_stride * (fy - 1);
-    const uint32_t a = __ldg(reinterpret_cast<const uint32_t*>(r0));
-    const uint32_t b = __ldg(reinterpret_cast<const uint32_t*>(r0 + 4 * (fx - 1)));
-    const uint32_t c = __ldg(reinterpret_cast<const uint32_t*>(r1));
-    const uint32_t d = __ldg(reinterpret_cast<const uint32_t*>(r1 + 4 * (fx - 1)));
+    uint32_t a, b, c, d;
+    if constexpr (PAIR) {
+        const uint2 p = __ldg(reinterpret_cast<const uint2*>(r0)), q = __ldg(reinterpret_cast<const uint2*>(r1));
+        a = p.x;
+        b = p.y;
+        c = q.x;
+        d = q.y;
+    } else {
+        a = __ldg(reinterpret_cast<const uint32_t*>(r0));
+        b = __ldg(reinterpret_cast<const uint32_t*>(r0 + 4 * (fx - 1)));
+        c = __ldg(reinterpret_cast<const uint32_t*>(r1));
+        d = __ldg(reinterpret_cast<const uint32_t*>(r1 + 4 * (fx - 1)));
+    }
     *reinterpret_cast<uint32_t*>(dst + (size_t)y * dst_stride + 4u * (size_t)x) = box4(a, b, c, d);
 }
 
+// Up to 6 levels per launch: a CTA takes a tile of up to 64x64 pixels of the
+// level above, writes its share of the first new level from two 8-byte row
+// loads per output pixel (all issued before any result is needed), keeps it
+// in shared memory and derives the following levels there (ping-pong
+// buffers), writing each to its place in the arena.  Used while both axes
+// halve; each level is the same box4 of the level above as in the one-level
+// kernel, so the results are identical.  (A resident grid looping over tiles
+// with the next tile's loads in flight measured slower: the hardware overlaps
+// the many short CTAs better.)
+struct MipOut {
+    uint8_t* data[6];
+    uint32_t pitch[6];
+};
+
+__global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restrict__ src, size_t src_stride,
+                                                        uint32_t tw_log2, uint32_t th_log2, uint32_t nlev, MipOut out)
+{
+    __shared__ uint32_t buf[2][32 * 32];
+    const uint32_t tx = blockIdx.x, ty = blockIdx.y;
+    uint32_t cw_log2 = tw_log2 - 1, ch_log2 = th_log2 - 1;  // tile size at the first new level
+    const uint8_t* tile = src + ((size_t)ty << th_log2) * src_stride + ((size_t)tx << tw_log2) * 4u;
+    // first level: up to 4 output pixels per thread (a 32x32 tile over 256 threads)
+    const uint32_t count = 1u << (cw_log2 + ch_log2);
+    uint2 p[4], q[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t i = threadIdx.x + 256u * k;
+        if (i < count) {
+            const uint32_t ox = i & ((1u << cw_log2) - 1u), oy = i >> cw_log2;
+            const uint8_t* r0 = tile + (size_t)(2u * oy) * src_stride + 8u * ox;
+            p[k] = __ldg(reinterpret_cast<const uint2*>(r0));
+            q[k] = __ldg(reinterpret_cast<const uint2*>(r0 + src_stride));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t i = threadIdx.x + 256u * k;
+        if (i < count) {
+            const uint32_t ox = i & ((1u << cw_log2) - 1u), oy = i >> cw_log2;
+            const uint32_t v = box4(p[k].x, p[k].y, q[k].x, q[k].y);
+            buf[0][i] = v;
+            *reinterpret_cast<uint32_t*>(out.data[0] + (size_t)((ty << ch_log2) + oy) * out.pitch[0] +
+                                         4u * ((tx << cw_log2) + ox)) = v;
+        }
+    }
+    for (uint32_t l = 1; l < nlev; ++l) {
+        __syncthreads();
+        const uint32_t* in = buf[(l - 1) & 1];
+        uint32_t* next = buf[l & 1];
+        const uint32_t nw_log2 = cw_log2 - 1, nh_log2 = ch_log2 - 1, cw = 1u << cw_log2;
+        for (uint32_t i = threadIdx.x; i < (1u << (nw_log2 + nh_log2)); i += 256u) {
+            const uint32_t ox = i & ((1u << nw_log2) - 1u), oy = i >> nw_log2;
+            const uint32_t* r0 = in + (2u * oy) * cw + 2u * ox;
+            const uint32_t v = box4(r0[0], r0[1], r0[cw], r0[cw + 1]);
+            next[i] = v;
+            *reinterpret_cast<uint32_t*>(out.data[l] + (size_t)((ty << nh_log2) + oy) * out.pitch[l] +
+                                         4u * ((tx << nw_log2) + ox)) = v;
+        }
+        cw_log2 = nw_log2;
+        ch_log2 = nh_log2;
+    }
+}
+
 bool pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+uint32_t log2u(uint32_t v)
+{
+    uint32_t l = 0;
+    while (v > 1) {
+        v >>= 1;
+        ++l;
+    }
+    return l;
+}
 
 size_t pitch_of(uint32_t w) { return ((size_t)4 * w + 255) & ~(size_t)255; }
 
@@ -88,16 +175,48 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     levels[0] = goofy_gpu_level{const_cast<void*>(src), width, height, stride};
     uint8_t* out = static_cast<uint8_t*>(arena);
-    for (uint32_t i = 1; i < n; ++i) {
+    for (uint32_t i = 1; i < n; ++i) {  // the arena layout: levels 1.. back to back, 256-byte rows
         const goofy_gpu_level& up = levels[i - 1];
         const uint32_t dw = up.width / 2 >= 4 ? up.width / 2 : 4, dh = up.height / 2 >= 4 ? up.height / 2 : 4;
-        const uint32_t fx = up.width > dw ? 2 : 1, fy = up.height > dh ? 2 : 1;
         const size_t pitch = pitch_of(dw);
-        mip_level_kernel<<<dim3((dw + 255) / 256, dh), 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
-                                                                      out, pitch, dw, dh, fx, fy);
-        GOOFY_CUDA_TRY(cudaGetLastError());
         levels[i] = goofy_gpu_level{out, dw, dh, (uint32_t)pitch};
         out += pitch * dh;
+    }
+    for (uint32_t i = 1; i < n;) {
+        const goofy_gpu_level& up = levels[i - 1];
+        // levels from here on that halve both axes (an axis at 4 stays 4)
+        uint32_t both = 0;
+        for (uint32_t w = up.width, h = up.height; i + both < n && w > 4 && h > 4; w /= 2, h /= 2) ++both;
+        const uint32_t tw = up.width < 64 ? up.width : 64, th = up.height < 64 ? up.height : 64;
+        uint32_t f = log2u(tw < th ? tw : th);
+        f = f < both ? f : both;
+        f = f < 6 ? f : 6;
+        if (f >= 2 && reinterpret_cast<uintptr_t>(up.data) % 8 == 0 && up.stride % 8 == 0) {
+            MipOut mo{};
+            for (uint32_t l = 0; l < f; ++l) {
+                mo.data[l] = static_cast<uint8_t*>(levels[i + l].data);
+                mo.pitch[l] = levels[i + l].stride;
+            }
+            mip_fused_kernel<<<dim3(up.width / tw, up.height / th), 256, 0, st>>>(
+                static_cast<const uint8_t*>(up.data), up.stride, log2u(tw), log2u(th), f, mo);
+            GOOFY_CUDA_TRY(cudaGetLastError());
+            i += f;
+            continue;
+        }
+        const goofy_gpu_level& lv = levels[i];
+        const uint32_t fx = up.width > lv.width ? 2 : 1, fy = up.height > lv.height ? 2 : 1;
+        const bool pair = fx == 2 && reinterpret_cast<uintptr_t>(up.data) % 8 == 0 && up.stride % 8 == 0;
+        const dim3 grid((lv.width + 255) / 256, lv.height);
+        if (pair)
+            mip_level_kernel<true><<<grid, 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
+                                                         static_cast<uint8_t*>(lv.data), lv.stride, lv.width,
+                                                         lv.height, fx, fy);
+        else
+            mip_level_kernel<false><<<grid, 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
+                                                          static_cast<uint8_t*>(lv.data), lv.stride, lv.width,
+                                                          lv.height, fx, fy);
+        GOOFY_CUDA_TRY(cudaGetLastError());
+        ++i;
     }
     *nlevels = n;
     return GOOFY_OK;

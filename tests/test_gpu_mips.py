@@ -19,7 +19,8 @@ def _host_chain(img, w, h):
     return out
 
 
-@pytest.mark.parametrize("w,h", [(4, 4), (8, 4), (64, 64), (256, 32), (16, 1024), (2048, 2048)])
+@pytest.mark.parametrize("w,h", [(4, 4), (8, 4), (8, 8), (16, 16), (64, 64), (256, 32), (16, 1024), (4096, 64),
+                                 (2048, 2048)])
 def test_device_mips_equal_host_chain(cuda, w, h):
     img = workloads.scene(w, h, w + h)
     host = _host_chain(img, w, h)
