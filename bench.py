@@ -209,6 +209,38 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
 
 
+def run_pair(args, g, torch, src, dst, codecs, stream, device):
+    """The timed step's two images (BC1 of one copy, ETC1s of the other) in
+    one batch launch instead of two image launches: the bandwidth-bound BC1
+    blocks and the ALU-bound ETC1s blocks share the GPU.  Outputs checked
+    against the image kernels' blocks."""
+    sh = stream.cuda_stream
+    outs = [torch.empty_like(dst[c]) for c in codecs]
+    arr = g.images_array([(src[c].data_ptr(), outs[c].data_ptr(), W, H, 4 * W, c) for c in codecs])
+    b = g.Batch(2, device)
+    try:
+        if not args.no_autotune:
+            b.autotune(arr, reps=3)
+        for _ in range(3):
+            assert b.encode(arr, sh) == g.OK, g.last_error()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.encode(arr, sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        tile = list(b.get_tile())
+    finally:
+        b.close()
+    px = 2 * W * H
+    return {"api": "goofy_gpu_batch_encode: both 8192x8192 images in one launch (CUDA-graph replay)",
+            "ms_per_step": round(ms, 4), "mpix_s": round(px / (ms / 1e3) / 1e6, 1),
+            "hbm_gbs": round(ALG_BYTES_PER_PX * px / (ms / 1e3) / 1e9, 1), "tile": tile,
+            "bit_exact_vs_image_kernels": all(bool(torch.equal(outs[c], dst[c])) for c in codecs)}
+
+
 def run_mips(g, torch, workloads, img, d_src, stream):
     """Device mip chain of the 8192x8192 image (levels 4096x4096 .. 4x4; up to
     6 levels per launch): median time, HBM rate for the algorithmic bytes (the
@@ -658,6 +690,7 @@ def run_gpu(args):
                              "decode_error_kernel_us": round(ms * 1e3, 2),
                              "decode_error_hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
     mips = run_mips(g, torch, workloads, img, src[0], stream)
+    pair = run_pair(args, g, torch, src, dst, codecs, stream, local)
     batched = None
     if not args.no_batched:
         batched = run_batched(args, g, torch, stream, dev)
@@ -676,7 +709,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
