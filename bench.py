@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=1.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
+    p.add_argument("--profile", choices=["encode", "quality", "mips"],
+                   help="only run a few launches of one kernel family (for ncu captures) and exit")
+    p.add_argument("--profile-size", type=int, default=4096, help="image side for --profile")
     return p.parse_args()
 
 
@@ -720,8 +723,50 @@ def run_gpu(args):
     return 0
 
 
+def run_profile(args):
+    """A few launches of one kernel family on a --profile-size square scene,
+    default tiles, nothing timed: the workload of the ncu captures under
+    profiles/ (small enough for a full capture to end in a minute)."""
+    import numpy as np
+    import torch
+
+    import goofy_gb300 as g
+    from goofy_gb300 import build as lib_build
+    from goofy_gb300 import workloads
+
+    lib_build.build()
+    assert g.init(0) == g.OK, g.last_error()
+    n = args.profile_size
+    img = workloads.scene(n, n, SEED, n // 256, max(8, n * n // 32768), threads=0)
+    src = torch.from_numpy(img.reshape(-1)).cuda()
+    sh = torch.cuda.current_stream().cuda_stream
+    dst = [torch.empty(g.out_size(n, n), dtype=torch.uint8, device="cuda") for _ in range(2)]
+    for c in (g.CODEC_BC1, g.CODEC_ETC1S):
+        for _ in range(3 if args.profile == "encode" else 1):
+            assert g.compress_device(c, dst[c].data_ptr(), src.data_ptr(), n, n, 4 * n, sh) == g.OK, g.last_error()
+    if args.profile == "quality":
+        sums = torch.zeros(6, dtype=torch.int64, device="cuda")
+        rgba = torch.empty(n * n * 4, dtype=torch.uint8, device="cuda")
+        bad = torch.zeros(1, dtype=torch.int64, device="cuda")
+        for c in (g.CODEC_BC1, g.CODEC_ETC1S):
+            for _ in range(3):
+                assert g.block_error_device(c, dst[c], src, n, n, 4 * n, sums, sh) == g.OK, g.last_error()
+            assert g.decode_device(c, rgba, 4 * n, dst[c], n, n, bad, sh) == g.OK, g.last_error()
+    if args.profile == "mips":
+        nbytes = g.lib().goofy_gpu_mip_arena_bytes(n, n)
+        arena = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
+        base = arena.data_ptr() + (-arena.data_ptr()) % 256
+        for _ in range(3):
+            g.generate_mips(src, n, n, 4 * n, base, nbytes, sh)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "size": n, "pipeline_timeouts": g.pipeline_timeouts()}))
+    return 0
+
+
 def main():
     args = parse()
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
