@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--serve-seconds", type=float, default=1.0, help="length of each offered-load run")
+    p.add_argument("--serve-seconds", type=float, default=2.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     p.add_argument("--profile", choices=["encode", "quality", "mips"],
@@ -401,6 +401,17 @@ def run_serving(args, g, device):
             off += (nb + 255) // 256 * 256
         return reqs, arrival, np.array([w * h for (w, h) in wh], np.int64), probe
 
+    def tail_phases(lat_ns, stamps):
+        """Where the slowest 1% of requests spent their time (means, ms):
+        submitted late (the submitting thread behind schedule), queued before
+        admission, admitted before launch, launch to completion."""
+        tail = lat_ns >= np.percentile(lat_ns, 99)
+        sub, adm, lau, done = (stamps[tail, k].astype(np.float64) for k in range(4))
+        sched = done - lat_ns[tail]
+        return {k: round(float(v.mean()) / 1e6, 3) for k, v in
+                (("submit_late", sub - sched), ("queued", adm - sub), ("admitted", lau - adm),
+                 ("launch_to_done", done - lau))}
+
     def classes(px, probe, lat_ns):
         out = {}
         groups = {"probe_1024x1024": probe, "small_le_128x128": (~probe) & (px <= 128 * 128),
@@ -437,14 +448,14 @@ def run_serving(args, g, device):
                     rate = f * cap / float(px.mean())
                     n = max(200, int(rate * args.serve_seconds))
                     reqs, arrival, rpx, rprobe = stream(n, rate)
-                    rc, lat, wall = srv.replay(reqs, arrival)
+                    rc, lat, wall, stamps = srv.replay(reqs, arrival, with_times=True)
                     assert rc == g.OK, g.last_error()
                     loads["%d%%" % round(100 * f)] = {
                         "offered_mpix_s": round(f * cap / 1e6, 1), "requests": n,
                         "sustained_mpix_s": round(float(rpx.sum()) / (wall / 1e9) / 1e6, 1),
                         "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
                         "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
-                        "by_class": classes(rpx, rprobe, lat)}
+                        "by_class": classes(rpx, rprobe, lat), "p99_tail_phases_ms": tail_phases(lat, stamps)}
                 entry["loads"] = loads
                 entry["stats"] = srv.stats()
                 result[name] = entry

@@ -154,7 +154,8 @@ def _declare(lib):
         "goofy_gpu_server_wait": (ctypes.c_int, [_VP, ctypes.c_uint64, _U32, ctypes.POINTER(RequestTimes)]),
         "goofy_gpu_server_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServerStats)]),
         "goofy_gpu_now_ns": (ctypes.c_int64, []),
-        "goofy_gpu_server_replay": (ctypes.c_int, [_VP, ctypes.POINTER(Request), _VP, _U32, _VP, ctypes.POINTER(ctypes.c_int64)]),
+        "goofy_gpu_server_replay": (ctypes.c_int, [_VP, ctypes.POINTER(Request), _VP, _U32, _VP, ctypes.POINTER(ctypes.c_int64),
+                                                   _VP]),
         "goofy_gpu_plain_replay": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Request), _VP, _U32, _VP,
                                                   ctypes.POINTER(ctypes.c_int64)]),
     }
@@ -415,17 +416,20 @@ class Server:
         assert lib().goofy_gpu_server_get_stats(self._h, ctypes.byref(st)) == OK
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
 
-    def replay(self, reqs, arrival_ns):
-        """Open-loop replay; returns (status, latency_ns int64 array, wall_ns)."""
+    def replay(self, reqs, arrival_ns, with_times=False):
+        """Open-loop replay; returns (status, latency_ns int64 array, wall_ns)
+        and, with `with_times`, an (n, 4) int64 array of submit / admit /
+        launch / done stamps."""
         import numpy as np
 
         arr = reqs if isinstance(reqs, ctypes.Array) else requests_array(reqs)
         arrival = np.ascontiguousarray(arrival_ns, dtype=np.int64)
         lat = np.zeros(len(arr), np.int64)
         wall = ctypes.c_int64()
+        times = np.zeros((len(arr), 4), np.int64) if with_times else None
         rc = lib().goofy_gpu_server_replay(self._h, arr, arrival.ctypes.data, len(arr), lat.ctypes.data,
-                                           ctypes.byref(wall))
-        return rc, lat, wall.value
+                                           ctypes.byref(wall), None if times is None else times.ctypes.data)
+        return (rc, lat, wall.value, times) if with_times else (rc, lat, wall.value)
 
     def close(self):
         if self._h:

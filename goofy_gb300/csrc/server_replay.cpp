@@ -32,7 +32,8 @@ void wait_until(int64_t t_ns)
 extern "C" {
 
 GOOFY_EXPORT int goofy_gpu_server_replay(goofy_gpu_server* s, const goofy_gpu_request* reqs, const int64_t* arrival_ns,
-                                         uint32_t n, int64_t* latency_ns, int64_t* wall_ns)
+                                         uint32_t n, int64_t* latency_ns, int64_t* wall_ns,
+                                         goofy_gpu_request_times* times)
 {
     if (!s || !reqs || !arrival_ns || !latency_ns || n == 0) return GOOFY_ERR_INVALID;
     std::vector<uint64_t> tickets(n, 0);
@@ -43,7 +44,11 @@ GOOFY_EXPORT int goofy_gpu_server_replay(goofy_gpu_server* s, const goofy_gpu_re
     std::thread collector([&] {
         for (uint32_t i = 0; i < n; ++i) {
             int st;
-            while ((st = ready[i].load(std::memory_order_acquire)) == 0) std::this_thread::yield();
+            // the latency comes from the completion timestamp, so this thread
+            // may lag; it sleeps rather than spin so it takes no core from the
+            // submitting and scheduling threads
+            while ((st = ready[i].load(std::memory_order_acquire)) == 0)
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
             if (st < 0) {
                 latency_ns[i] = -1;
                 continue;
@@ -57,13 +62,14 @@ GOOFY_EXPORT int goofy_gpu_server_replay(goofy_gpu_server* s, const goofy_gpu_re
                 continue;
             }
             latency_ns[i] = t.done_ns - (t0 + arrival_ns[i]);
+            if (times) times[i] = t;
         }
     });
     for (uint32_t i = 0; i < n; ++i) {
         wait_until(t0 + arrival_ns[i]);
         int rc;
         while ((rc = goofy_gpu_server_submit(s, &reqs[i], &tickets[i])) == GOOFY_ERR_BUSY)
-            std::this_thread::yield();  // ticket ring full: the collector releases tickets as it goes
+            std::this_thread::sleep_for(std::chrono::microseconds(20));  // ticket ring full: the collector releases tickets
         if (rc != GOOFY_OK) {
             int expected = GOOFY_OK;
             first_error.compare_exchange_strong(expected, rc);

@@ -336,9 +336,10 @@ int64_t goofy_gpu_now_ns(void);
 
 /* Open-loop load replay: submits reqs[i] at start + arrival_ns[i] while a
  * second thread waits on the tickets; latency_ns[i] = completion - scheduled
- * arrival (-1 if it failed); wall_ns = start to last completion. */
+ * arrival (-1 if it failed); wall_ns = start to last completion; times (may be
+ * NULL) receives each request's submit / admit / launch / completion stamps. */
 int goofy_gpu_server_replay(goofy_gpu_server* server, const goofy_gpu_request* reqs, const int64_t* arrival_ns,
-                            uint32_t n, int64_t* latency_ns, int64_t* wall_ns);
+                            uint32_t n, int64_t* latency_ns, int64_t* wall_ns, goofy_gpu_request_times* times);
 
 /* The same replay through the plain loop: one request at a time, each a
  * host->device copy, one image-kernel launch and a device->host copy. */

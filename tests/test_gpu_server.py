@@ -138,8 +138,12 @@ def test_replay_and_plain_loop(cuda, mode):
     arrival = np.cumsum(rng.exponential(20e3, len(reqs))).astype(np.int64)  # ~50k requests/s
     srv = g.Server(mode=mode)
     try:
-        rc, lat, wall = srv.replay(arr, arrival)
+        rc, lat, wall, stamps = srv.replay(arr, arrival, with_times=True)
         assert rc == g.OK and (lat > 0).all() and wall > 0
+        # submit <= admit <= launch <= done for every request, done - latency = its scheduled arrival
+        assert (np.diff(stamps, axis=1) >= 0).all()
+        sched = stamps[:, 3] - lat
+        np.testing.assert_array_equal(np.diff(sched), np.diff(arrival))
         for r in reqs:
             np.testing.assert_array_equal(r["dst"], alone(r))
             r["dst"][:] = 0
