@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--serve-seconds", type=float, default=2.0, help="length of each offered-load run")
+    p.add_argument("--serve-seconds", type=float, default=4.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     p.add_argument("--profile", choices=["encode", "quality", "mips"],
@@ -455,6 +455,8 @@ def run_serving(args, g, device):
                         "sustained_mpix_s": round(float(rpx.sum()) / (wall / 1e9) / 1e6, 1),
                         "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
                         "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
+                        "p999_ms": round(float(np.percentile(lat, 99.9)) / 1e6, 3),
+                        "max_ms": round(float(lat.max()) / 1e6, 3),
                         "by_class": classes(rpx, rprobe, lat), "p99_tail_phases_ms": tail_phases(lat, stamps)}
                 entry["loads"] = loads
                 entry["stats"] = srv.stats()

@@ -56,62 +56,69 @@ __global__ void __launch_bounds__(256) mip_level_kernel(const uint8_t* __restric
 }
 
 // Up to 6 levels per launch: a CTA takes a tile of up to 64x64 pixels of the
-// level above, writes its share of the first new level from two 8-byte row
-// loads per output pixel (all issued before any result is needed), keeps it
-// in shared memory and derives the following levels there (ping-pong
-// buffers), writing each to its place in the arena.  Used while both axes
-// halve; each level is the same box4 of the level above as in the one-level
-// kernel, so the results are identical.  (A resident grid looping over tiles
-// with the next tile's loads in flight measured slower: the hardware overlaps
-// the many short CTAs better.)
+// level above.  Each thread reads a 4x4 patch (four 16-byte row loads), makes
+// the 2x2 quad of the first new level and the one pixel of the second from it
+// in registers, the third level comes from the 2x2 neighbourhood of second-
+// level pixels held by lanes t^1, t^w, t^w^1 of the same warp (shuffles), and
+// the remaining levels (at most 8x8 pixels per tile) go through shared
+// memory.  Used while both axes halve; every level is the same box4 of the
+// level above as in the one-level kernel, so the results are identical.
 struct MipOut {
     uint8_t* data[6];
     uint32_t pitch[6];
 };
 
+__device__ __forceinline__ void store_px(const MipOut& o, int l, uint32_t row, uint32_t col, uint32_t v)
+{
+    *reinterpret_cast<uint32_t*>(o.data[l] + (size_t)row * o.pitch[l] + 4u * col) = v;
+}
+
 __global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restrict__ src, size_t src_stride,
                                                         uint32_t tw_log2, uint32_t th_log2, uint32_t nlev, MipOut out)
 {
-    __shared__ uint32_t buf[2][32 * 32];
-    const uint32_t tx = blockIdx.x, ty = blockIdx.y;
-    uint32_t cw_log2 = tw_log2 - 1, ch_log2 = th_log2 - 1;  // tile size at the first new level
-    const uint8_t* tile = src + ((size_t)ty << th_log2) * src_stride + ((size_t)tx << tw_log2) * 4u;
-    // first level: up to 4 output pixels per thread (a 32x32 tile over 256 threads)
-    const uint32_t count = 1u << (cw_log2 + ch_log2);
-    uint2 p[4], q[4];
+    __shared__ uint32_t buf[2][64];
+    const uint32_t tx = blockIdx.x, ty = blockIdx.y, t = threadIdx.x;
+    // second-level tile: (tw/4) x (th/4) pixels, one per thread
+    const uint32_t w2_log2 = tw_log2 - 2, h2_log2 = th_log2 - 2, w2 = 1u << w2_log2;
+    const bool act = t < (1u << (w2_log2 + h2_log2));
+    const uint32_t x2 = t & (w2 - 1u), y2 = t >> w2_log2;
+    uint32_t v2 = 0;
+    if (act) {
+        const uint8_t* patch = src + (((size_t)ty << th_log2) + 4u * y2) * src_stride +
+                               (((size_t)tx << tw_log2) + 4u * x2) * 4u;
+        uint4 r[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint32_t i = threadIdx.x + 256u * k;
-        if (i < count) {
-            const uint32_t ox = i & ((1u << cw_log2) - 1u), oy = i >> cw_log2;
-            const uint8_t* r0 = tile + (size_t)(2u * oy) * src_stride + 8u * ox;
-            p[k] = __ldg(reinterpret_cast<const uint2*>(r0));
-            q[k] = __ldg(reinterpret_cast<const uint2*>(r0 + src_stride));
-        }
+        for (int k = 0; k < 4; ++k) r[k] = __ldg(reinterpret_cast<const uint4*>(patch + (size_t)k * src_stride));
+        const uint32_t q00 = box4(r[0].x, r[0].y, r[1].x, r[1].y), q01 = box4(r[0].z, r[0].w, r[1].z, r[1].w);
+        const uint32_t q10 = box4(r[2].x, r[2].y, r[3].x, r[3].y), q11 = box4(r[2].z, r[2].w, r[3].z, r[3].w);
+        const uint32_t row1 = (ty << (th_log2 - 1)) + 2u * y2, col1 = (tx << (tw_log2 - 1)) + 2u * x2;
+        *reinterpret_cast<uint2*>(out.data[0] + (size_t)row1 * out.pitch[0] + 4u * col1) = make_uint2(q00, q01);
+        *reinterpret_cast<uint2*>(out.data[0] + (size_t)(row1 + 1) * out.pitch[0] + 4u * col1) = make_uint2(q10, q11);
+        v2 = box4(q00, q01, q10, q11);
+        if (nlev > 1) store_px(out, 1, (ty << h2_log2) + y2, (tx << w2_log2) + x2, v2);
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint32_t i = threadIdx.x + 256u * k;
-        if (i < count) {
-            const uint32_t ox = i & ((1u << cw_log2) - 1u), oy = i >> cw_log2;
-            const uint32_t v = box4(p[k].x, p[k].y, q[k].x, q[k].y);
-            buf[0][i] = v;
-            *reinterpret_cast<uint32_t*>(out.data[0] + (size_t)((ty << ch_log2) + oy) * out.pitch[0] +
-                                         4u * ((tx << cw_log2) + ox)) = v;
-        }
+    if (nlev <= 2) return;
+    // third level: lanes with even x2 and y2 combine their 2x2 neighbourhood
+    const uint32_t b = __shfl_xor_sync(0xffffffffu, v2, 1), c = __shfl_xor_sync(0xffffffffu, v2, w2),
+                   d = __shfl_xor_sync(0xffffffffu, v2, w2 ^ 1u);
+    const uint32_t w3_log2 = w2_log2 - 1, h3_log2 = h2_log2 - 1;
+    if (act && !(x2 & 1u) && !(y2 & 1u)) {
+        const uint32_t v3 = box4(v2, b, c, d), x3 = x2 >> 1, y3 = y2 >> 1;
+        store_px(out, 2, (ty << h3_log2) + y3, (tx << w3_log2) + x3, v3);
+        buf[0][(y3 << w3_log2) + x3] = v3;
     }
-    for (uint32_t l = 1; l < nlev; ++l) {
+    uint32_t cw_log2 = w3_log2, ch_log2 = h3_log2;
+    for (uint32_t l = 3; l < nlev; ++l) {
         __syncthreads();
-        const uint32_t* in = buf[(l - 1) & 1];
-        uint32_t* next = buf[l & 1];
+        const uint32_t* in = buf[(l - 3) & 1];
+        uint32_t* next = buf[(l - 2) & 1];
         const uint32_t nw_log2 = cw_log2 - 1, nh_log2 = ch_log2 - 1, cw = 1u << cw_log2;
-        for (uint32_t i = threadIdx.x; i < (1u << (nw_log2 + nh_log2)); i += 256u) {
-            const uint32_t ox = i & ((1u << nw_log2) - 1u), oy = i >> nw_log2;
+        if (t < (1u << (nw_log2 + nh_log2))) {
+            const uint32_t ox = t & ((1u << nw_log2) - 1u), oy = t >> nw_log2;
             const uint32_t* r0 = in + (2u * oy) * cw + 2u * ox;
             const uint32_t v = box4(r0[0], r0[1], r0[cw], r0[cw + 1]);
-            next[i] = v;
-            *reinterpret_cast<uint32_t*>(out.data[l] + (size_t)((ty << nh_log2) + oy) * out.pitch[l] +
-                                         4u * ((tx << nw_log2) + ox)) = v;
+            next[t] = v;
+            store_px(out, (int)l, (ty << nh_log2) + oy, (tx << nw_log2) + ox, v);
         }
         cw_log2 = nw_log2;
         ch_log2 = nh_log2;
@@ -191,7 +198,7 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
         uint32_t f = log2u(tw < th ? tw : th);
         f = f < both ? f : both;
         f = f < 6 ? f : 6;
-        if (f >= 2 && reinterpret_cast<uintptr_t>(up.data) % 8 == 0 && up.stride % 8 == 0) {
+        if (f >= 2 && reinterpret_cast<uintptr_t>(up.data) % 16 == 0 && up.stride % 16 == 0) {
             MipOut mo{};
             for (uint32_t l = 0; l < f; ++l) {
                 mo.data[l] = static_cast<uint8_t*>(levels[i + l].data);
