@@ -215,7 +215,7 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     const uint32_t t_lo = min(max(4 * ((int)br.mid - (int)br.qt) + 1, 0), 1021);
     const uint32_t t_hi = min(4u * (br.mid + br.qt) - 3u, 1021u);
     const uint32_t k_q = (2048u - t_gez) | (2048u - t_lo) << 16;
-    const uint32_t k_d = ((t_lo - t_hi) << 16) - (2048u - t_gez);  // q + k_d: low lane S, high lane S + 2048 - t_hi
+    const uint32_t k_h = (2048u - t_hi) << 16;  // h: low lane S, high lane S + 2048 - t_hi
     uint32_t group[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int y = 0; y < 4; ++y)
@@ -226,7 +226,7 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
             const int m = j >= 11 ? j - 11 : j >= 6 ? j - 6 : j >= 1 ? j - 1 : 0;
             const uint32_t s = luma_sum(w[4 * y + x], 0u);
             const uint32_t q = s * (0x00010001u << m) + (k_q << m);  // bit 11+m: Y >= mid, 27+m: Y >= mid-qt+1
-            const uint32_t h = q + (k_d << m);                        // bit 27+m: Y >= mid+qt; bit 11+m clear
+            const uint32_t h = s * (0x00010001u << m) + (k_h << m);  // bit 27+m: Y >= mid+qt; bit 11+m clear
             group[gi] += (~q | h) & (0x08000800u << m);
         }
     const uint32_t word1 = group[0] + (group[1] >> 5) + (group[2] >> 10) + (group[3] >> 11);
