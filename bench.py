@@ -23,6 +23,7 @@ they exist, else the oracle port of it), with every host thread.
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -180,6 +181,24 @@ def cpu_encode_all(lib_fn, img, threads, outs=None):
     return time.perf_counter() - t0
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu / /proc/cpuinfo), for the baseline's label."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(img, gpu_outputs, budget_s=12.0):
     """Oracle port (or the compiled reference where present) on this host's
     cores: all threads, best of a few full-image passes of both codecs.  The
@@ -209,6 +228,7 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
                       % (len(times), cores),
             "single_thread_mpix_s": round(px / t1 / 1e6, 1),
             "median_mpix_s": round(px / statistics.median(times) / 1e6, 1),
+            "cpu": "%s, %s" % (cpu_model(), platform.machine()),
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
 
 
@@ -515,6 +535,7 @@ def run_reference(args):
                        "implementation": "reference encoder compiled from its sources" if kind == "reference"
                        else "oracle port of the reference encoder (reference sources absent on this host)"},
             "cpu_baseline": {"value": round(value, 1), "unit": "MPix/s", "cores": cores, "kind": kind,
+                             "cpu": "%s, %s" % (cpu_model(), platform.machine()),
                              "sample": "full 8192x8192 image per step, BC1 + ETC1s, block rows striped over "
                                        "%d threads" % cores},
             "e2e": {"value": round(value, 1), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
