@@ -483,6 +483,20 @@ def run_serving(args, g, device):
                 result[name] = entry
             finally:
                 srv.close()
+        # the staged server with per-request quality (RGB PSNR of every request, measured on the GPU)
+        srv = g.Server(mode=g.SERVER_STAGED, device=device, quality=True)
+        try:
+            reqs, arrival, px, _ = stream(20000, None)
+            srv.replay(reqs[:2000], arrival[:2000])
+            rc, lat, wall, _ = srv.replay(reqs, arrival, with_times=True)
+            assert rc == g.OK, g.last_error()
+            ps = srv.last_psnr
+            result["staged_with_quality"] = {
+                "capacity_mpix_s": round(float(px.sum()) / (wall / 1e9) / 1e6, 1), "requests": len(reqs),
+                "psnr_rgb_db_mean": round(float(ps.mean()), 4), "psnr_rgb_db_min": round(float(ps.min()), 4),
+                "note": "one more launch per batch decodes the fresh blocks and sums the harness's errors"}
+        finally:
+            srv.close()
         n_plain = 4000
         reqs, arrival, px, probe = stream(n_plain, None)
         rc, lat, wall = g.plain_replay(reqs, arrival, device)

@@ -56,7 +56,7 @@ SERVER_DIRECT = 1
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("mode", ctypes.c_int32), ("device_budget_bytes", ctypes.c_uint64),
                 ("max_batch_images", ctypes.c_uint32), ("max_inflight_batches", ctypes.c_uint32),
-                ("max_requests", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("max_requests", ctypes.c_uint32), ("quality", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -67,7 +67,7 @@ class Request(ctypes.Structure):
 
 class RequestTimes(ctypes.Structure):
     _fields_ = [("submit_ns", ctypes.c_int64), ("admit_ns", ctypes.c_int64), ("launch_ns", ctypes.c_int64),
-                ("done_ns", ctypes.c_int64)]
+                ("done_ns", ctypes.c_int64), ("psnr_rgb", ctypes.c_double)]
 
 
 class ServerStats(ctypes.Structure):
@@ -155,7 +155,7 @@ def _declare(lib):
         "goofy_gpu_server_get_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ServerStats)]),
         "goofy_gpu_now_ns": (ctypes.c_int64, []),
         "goofy_gpu_server_replay": (ctypes.c_int, [_VP, ctypes.POINTER(Request), _VP, _U32, _VP, ctypes.POINTER(ctypes.c_int64),
-                                                   _VP]),
+                                                   ctypes.POINTER(RequestTimes)]),
         "goofy_gpu_plain_replay": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Request), _VP, _U32, _VP,
                                                   ctypes.POINTER(ctypes.c_int64)]),
     }
@@ -386,10 +386,11 @@ class Server:
     """goofy_gpu_server: continuous-batching server for host-memory requests."""
 
     def __init__(self, mode=SERVER_STAGED, device_budget_bytes=16 << 30, max_batch_images=1024,
-                 max_inflight_batches=4, max_requests=1 << 20, device=0):
+                 max_inflight_batches=4, max_requests=1 << 20, device=0, quality=False):
         cfg = ServerConfig()
         lib().goofy_gpu_server_default_config(ctypes.byref(cfg))
         cfg.device, cfg.mode, cfg.device_budget_bytes = device, mode, device_budget_bytes
+        cfg.quality = 1 if quality else 0
         cfg.max_batch_images, cfg.max_inflight_batches, cfg.max_requests = (max_batch_images, max_inflight_batches,
                                                                             max_requests)
         h = ctypes.c_void_p()
@@ -426,10 +427,15 @@ class Server:
         arrival = np.ascontiguousarray(arrival_ns, dtype=np.int64)
         lat = np.zeros(len(arr), np.int64)
         wall = ctypes.c_int64()
-        times = np.zeros((len(arr), 4), np.int64) if with_times else None
+        times = (RequestTimes * len(arr))() if with_times else None
         rc = lib().goofy_gpu_server_replay(self._h, arr, arrival.ctypes.data, len(arr), lat.ctypes.data,
-                                           ctypes.byref(wall), None if times is None else times.ctypes.data)
-        return (rc, lat, wall.value, times) if with_times else (rc, lat, wall.value)
+                                           ctypes.byref(wall), times)
+        if not with_times:
+            return rc, lat, wall.value
+        raw = np.ctypeslib.as_array(times)
+        stamps = np.stack([raw[k] for k in ("submit_ns", "admit_ns", "launch_ns", "done_ns")], axis=1)
+        self.last_psnr = np.array(raw["psnr_rgb"])
+        return rc, lat, wall.value, stamps
 
     def close(self):
         if self._h:

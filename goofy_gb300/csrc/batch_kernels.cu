@@ -18,18 +18,6 @@
 
 namespace goofy_gpu {
 
-// Largest i < n with first_unit[i] <= u (first_unit[0] == 0, ascending).
-__device__ __forceinline__ uint32_t find_image(const uint32_t* first_unit, uint32_t n, uint32_t u)
-{
-    uint32_t lo = 0, hi = n;  // invariant: first_unit[lo] <= u < first_unit[hi] (first_unit[n] = inf)
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (first_unit[mid] <= u) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 template <int BPT>
 __global__ void __launch_bounds__(512) encode_batch_kernel(const BatchImage* __restrict__ images, uint32_t n_images,
                                                            const uint32_t* __restrict__ first_unit,

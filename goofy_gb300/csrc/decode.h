@@ -18,4 +18,13 @@ cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint
 cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* src, uint32_t width, uint32_t height,
                                size_t stride, bool vec16, unsigned long long* sums, cudaStream_t stream);
 
+struct BatchImage;
+
+// Adds the six error sums of every image of a batch (blocks at `dst`, source
+// at `src`) to sums[6 * i + c]; work units as for the batch encoder
+// (`first_unit`, `unit_blocks`), `work_counter` reading 0 at the start.
+cudaError_t launch_quality_batch(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,
+                                 uint32_t total_units, uint32_t unit_blocks, uint32_t* work_counter,
+                                 unsigned long long* sums, cudaStream_t stream);
+
 }  // namespace goofy_gpu

@@ -13,6 +13,7 @@
 // shuffles and shared memory, one 64-bit atomic per CTA and channel).
 #include <cuda_runtime.h>
 
+#include "batch.h"
 #include "block_codec.cuh"
 #include "block_decode.cuh"
 #include "decode.h"
@@ -125,6 +126,75 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
         for (uint32_t k = 0; k < (blockDim.x >> 5); ++k) t += part[threadIdx.x][k];
         if (t) atomicAdd(&sums[threadIdx.x], t);
     }
+}
+
+// The error sums of every image of a batch (the request server's quality
+// measurement): the batch's work units, pulled from a counter as in the
+// encoder's batch kernel, decode the image's blocks (`dst`) and compare them
+// with its source; a warp sums its unit and adds six totals to the image's
+// sums[6 * image + c].
+__global__ void __launch_bounds__(256) quality_batch_kernel(const BatchImage* __restrict__ images, uint32_t n_images,
+                                                            const uint32_t* __restrict__ first_unit,
+                                                            uint32_t total_units, uint32_t unit_blocks,
+                                                            uint32_t* __restrict__ work_counter,
+                                                            unsigned long long* __restrict__ sums)
+{
+    __shared__ uint32_t pal[8 * 256];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(work_counter, 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= total_units) return;
+        const uint32_t ii = find_image(first_unit, n_images, u);
+        const BatchImage im = images[ii];
+        const uint32_t first = (u - im.first_unit) * unit_blocks, last = min(first + unit_blocks, im.bw * im.bh);
+        // per lane at most 2048 blocks of a unit: 2048 * 16 * 255^2 < 2^32 per channel
+        uint32_t acc[4] = {0, 0, 0, 0}, bad = 0;
+        unsigned long long ys = 0;
+        for (uint32_t b = first + lane; b < last; b += 32u) {
+            uint32_t bx;
+            const uint32_t by = div_magic(b, im.bw, im.bw_magic, bx);
+            uint32_t px[16], w[16];
+            const uint2 blk = load_block8(im.dst + 8u * (size_t)b);
+            const bool ok = im.codec == kBC1 ? decode_block<kBC1>(blk, pal + threadIdx.x, blockDim.x, px)
+                                             : decode_block<kETC1S>(blk, pal + threadIdx.x, blockDim.x, px);
+            load_block_rows(im.src + (size_t)by * 4u * im.stride + 16u * (size_t)bx, im.stride, im.vec16 != 0, w);
+#pragma unroll
+            for (int y = 0; y < 4; ++y) {
+                const uint32_t a[4] = {w[4 * y], w[4 * y + 1], w[4 * y + 2], w[4 * y + 3]};
+                const uint32_t d[4] = {px[4 * y], px[4 * y + 1], px[4 * y + 2], px[4 * y + 3]};
+                accumulate_row(a, d, acc);
+                ys += luma_row(a, d);
+            }
+            bad += ok ? 0u : 1u;
+        }
+        unsigned long long t[6] = {acc[0], acc[1], acc[2], acc[3], bad, ys};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_xor_sync(0xffffffffu, t[c], o);
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+                if (t[c]) atomicAdd(&sums[6u * ii + c], t[c]);
+    }
+}
+
+cudaError_t launch_quality_batch(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,
+                                 uint32_t total_units, uint32_t unit_blocks, uint32_t* work_counter,
+                                 unsigned long long* sums, cudaStream_t stream)
+{
+    if (total_units == 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t warps = total_units, ctas = (warps + 7) / 8;
+    const uint32_t grid = (uint32_t)(ctas < (uint64_t)sms * 8u ? ctas : (uint64_t)sms * 8u);
+    quality_batch_kernel<<<grid, 256, 0, stream>>>(images, n_images, first_unit, total_units, unit_blocks,
+                                                   work_counter, sums);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint32_t height, uint8_t* rgba,

@@ -64,6 +64,19 @@ __device__ __forceinline__ uint32_t div_magic(uint32_t n, uint32_t d, uint32_t m
     return q;
 }
 
+// Largest i < n with first_unit[i] <= u (first_unit[0] == 0, ascending): the
+// image a work unit of a batch belongs to.
+__device__ __forceinline__ uint32_t find_image(const uint32_t* first_unit, uint32_t n, uint32_t u)
+{
+    uint32_t lo = 0, hi = n;  // invariant: first_unit[lo] <= u < first_unit[hi] (first_unit[n] = inf)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (first_unit[mid] <= u) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // etc1BrighnessRangeTocontrolByte (goofy_tc.h:1040-1057) as 128 bytes indexed by range >> 1.
 __device__ __forceinline__ void fill_ctrl_lut(uint8_t* lut)
 {

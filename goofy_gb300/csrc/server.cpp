@@ -17,6 +17,9 @@
 //     direct mode: the batch kernel reads the request's pinned source and
 //     writes its pinned destination itself over NVLink-C2C (one launch, no
 //     copy calls),
+//   * with config.quality, decodes each launch's fresh blocks on the GPU and
+//     sums the harness's squared errors per request (same work units, one
+//     more launch), so every request also gets its RGB PSNR,
 //   * releases arena space and launch slots when a launch's completion
 //     callback fires (cudaLaunchHostFunc), which also timestamps the requests.
 // A batch of size 1 with one launch slot is the plain one-request-per-launch
@@ -25,7 +28,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -36,6 +41,7 @@
 
 #include "../../include/goofy_gpu.h"
 #include "batch.h"
+#include "decode.h"
 #include "host_util.h"
 
 using goofy_gpu::BatchImage;
@@ -63,6 +69,7 @@ struct Request {
     int status = GOOFY_OK;
     int state = kFree;
     int64_t t_submit = 0, t_admit = 0, t_launch = 0, t_done = 0;
+    double psnr_rgb = 0.0;
 };
 
 // Device memory handed out in arrival order and returned roughly in order.
@@ -124,6 +131,8 @@ struct LaunchSlot {
     BatchImage* d_desc = nullptr;
     uint32_t* d_first = nullptr;
     uint32_t* d_counter = nullptr;
+    unsigned long long* d_qsums = nullptr;  // quality: 6 error sums per request
+    unsigned long long* h_qsums = nullptr;
     cudaEvent_t ev_in = nullptr, ev_kernel = nullptr;
     std::vector<uint64_t> tickets;
     bool busy = false;
@@ -182,8 +191,14 @@ void retire_locked(goofy_gpu_server* s)
 {
     for (int si : s->finished_slots) {
         LaunchSlot& sl = s->slots[si];
-        for (uint64_t tk : sl.tickets) {
-            Request& r = s->rec(tk);
+        for (size_t i = 0; i < sl.tickets.size(); ++i) {
+            Request& r = s->rec(sl.tickets[i]);
+            if (s->cfg.quality) {
+                // getPSNR(mseRGB, 768), Src/main.cpp:386-395, :455, :466
+                const unsigned long long* q = sl.h_qsums + 6 * i;
+                const double mse = (double)(q[0] + q[1] + q[2]) / ((double)r.req.width * (double)r.req.height);
+                r.psnr_rgb = mse < 0.0000001 ? DBL_MAX : 10.0 * std::log10((768.0 * 768.0) / mse);
+            }
             if (s->cfg.mode == GOOFY_SERVER_STAGED) s->arena.release(r.arena_off);
             s->inflight_bytes -= r.charge;
             r.state = kDone;
@@ -277,6 +292,14 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
                                                        (units * 32 + s->tile.threads - 1) / s->tile.threads);
     GOOFY_CUDA_TRY(goofy_gpu::launch_batch(sl.d_desc, n, sl.d_first, (uint32_t)units, sl.d_counter, s->tile,
                                            ctas ? ctas : 1, s->s_compute));
+    if (s->cfg.quality) {  // decode the fresh blocks and compare with each request's source, same units
+        GOOFY_CUDA_TRY(cudaMemsetAsync(sl.d_qsums, 0, 6 * sizeof(unsigned long long) * n, s->s_compute));
+        GOOFY_CUDA_TRY(cudaMemsetAsync(sl.d_counter, 0, sizeof(uint32_t), s->s_compute));
+        GOOFY_CUDA_TRY(goofy_gpu::launch_quality_batch(sl.d_desc, n, sl.d_first, (uint32_t)units, s->tile.unit_blocks,
+                                                       sl.d_counter, sl.d_qsums, s->s_compute));
+        GOOFY_CUDA_TRY(cudaMemcpyAsync(sl.h_qsums, sl.d_qsums, 6 * sizeof(unsigned long long) * n,
+                                       cudaMemcpyDeviceToHost, s->s_compute));
+    }
     cudaStream_t last = s->s_compute;
     if (staged) {
         GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_kernel, s->s_compute));
@@ -363,6 +386,11 @@ int init_server(goofy_gpu_server* s)
         GOOFY_CUDA_TRY(cudaMalloc(&sl.d_desc, sizeof(BatchImage) * c.max_batch_images));
         GOOFY_CUDA_TRY(cudaMalloc(&sl.d_first, sizeof(uint32_t) * c.max_batch_images));
         GOOFY_CUDA_TRY(cudaMalloc(&sl.d_counter, sizeof(uint32_t)));
+        if (c.quality) {
+            GOOFY_CUDA_TRY(cudaMalloc(&sl.d_qsums, 6 * sizeof(unsigned long long) * c.max_batch_images));
+            GOOFY_CUDA_TRY(cudaHostAlloc(&sl.h_qsums, 6 * sizeof(unsigned long long) * c.max_batch_images,
+                                         cudaHostAllocDefault));
+        }
         GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_in, cudaEventDisableTiming));
         GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_kernel, cudaEventDisableTiming));
     }
@@ -382,6 +410,8 @@ void teardown(goofy_gpu_server* s)
         if (sl.d_desc) cudaFree(sl.d_desc);
         if (sl.d_first) cudaFree(sl.d_first);
         if (sl.d_counter) cudaFree(sl.d_counter);
+        if (sl.d_qsums) cudaFree(sl.d_qsums);
+        if (sl.h_qsums) cudaFreeHost(sl.h_qsums);
         if (sl.ev_in) cudaEventDestroy(sl.ev_in);
         if (sl.ev_kernel) cudaEventDestroy(sl.ev_kernel);
     }
@@ -411,6 +441,7 @@ GOOFY_EXPORT int goofy_gpu_server_create(goofy_gpu_server** out, const goofy_gpu
     if (!out || !cfg) return GOOFY_ERR_INVALID;
     *out = nullptr;
     if (cfg->mode != GOOFY_SERVER_STAGED && cfg->mode != GOOFY_SERVER_DIRECT) return GOOFY_ERR_INVALID;
+    if (cfg->quality > 1) return GOOFY_ERR_INVALID;
     if (cfg->device_budget_bytes < (1u << 20) || cfg->max_batch_images == 0 || cfg->max_batch_images > 65536 ||
         cfg->max_inflight_batches == 0 || cfg->max_inflight_batches > 64 || cfg->max_requests < 16)
         return GOOFY_ERR_INVALID;
@@ -506,6 +537,7 @@ GOOFY_EXPORT int goofy_gpu_server_wait(goofy_gpu_server* s, uint64_t ticket, uin
         times->admit_ns = r.t_admit;
         times->launch_ns = r.t_launch;
         times->done_ns = r.t_done;
+        times->psnr_rgb = r.psnr_rgb;
     }
     const int status = r.status;
     r.state = kFree;  // the ticket is released

@@ -285,7 +285,7 @@ typedef struct goofy_gpu_server_config {
     uint32_t max_batch_images;     /* requests folded into one launch */
     uint32_t max_inflight_batches; /* launches on the GPU at once */
     uint32_t max_requests;         /* unreleased tickets at once */
-    uint32_t reserved;
+    uint32_t quality;              /* 1: measure every request's RGB PSNR on the GPU (harness's getMsePsnr) */
 } goofy_gpu_server_config;
 
 /* One encode request on host memory (pinned buffers are copied by DMA / read
@@ -299,6 +299,7 @@ typedef struct goofy_gpu_request {
 
 typedef struct goofy_gpu_request_times {
     int64_t submit_ns, admit_ns, launch_ns, done_ns; /* goofy_gpu_now_ns() clock */
+    double psnr_rgb; /* with config.quality: RGB PSNR of the blocks as the harness reports it (peak 768), else 0 */
 } goofy_gpu_request_times;
 
 typedef struct goofy_gpu_server_stats {

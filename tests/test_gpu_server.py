@@ -154,3 +154,38 @@ def test_replay_and_plain_loop(cuda, mode):
     finally:
         srv.close()
         free_requests(reqs)
+
+
+@pytest.mark.parametrize("mode", [g.SERVER_STAGED, g.SERVER_DIRECT])
+def test_quality_reports_each_requests_psnr(cuda, mode):
+    """With quality on, every request's RGB PSNR (measured on the GPU from the
+    batch's own blocks, in the same launches) equals the harness's figure for
+    that request alone: decode with the harness's decoder, getMsePsnr."""
+    rng = np.random.default_rng(33)
+    reqs = make_requests(rng, 40, True, max_side=512)
+    srv = g.Server(mode=mode, quality=True)
+    try:
+        tickets = [srv.submit(r["codec"], r["dst"], r["src"], r["w"], r["h"], r["stride"]) for r in reqs]
+        assert all(rc == g.OK for rc, _ in tickets)
+        for r, (_, tk) in zip(reqs, tickets):
+            rc, tm = srv.wait(tk)
+            assert rc == g.OK
+            blocks = alone(r)
+            np.testing.assert_array_equal(r["dst"], blocks)
+            dec, bad = oracle.decode(r["codec"], blocks, r["w"], r["h"])
+            src = np.ascontiguousarray(r["img"][:, :4 * r["w"]])
+            assert bad == 0
+            assert tm.psnr_rgb == oracle.psnr_rgb(oracle.sq_error(src, dec, r["w"], r["h"]), r["w"], r["h"])
+    finally:
+        srv.close()
+        free_requests(reqs)
+    # without quality the field stays 0
+    reqs = make_requests(rng, 4, True, max_side=64)
+    srv = g.Server(mode=mode)
+    try:
+        for r in reqs:
+            rc, tk = srv.submit(r["codec"], r["dst"], r["src"], r["w"], r["h"], r["stride"])
+            assert rc == g.OK and srv.wait(tk)[1].psnr_rgb == 0.0
+    finally:
+        srv.close()
+        free_requests(reqs)
