@@ -2,7 +2,7 @@
 
 ``load()`` returns the ctypes handle of the C restatement (goofy_oracle.c);
 ``load_ref()`` the reference encoder compiled from its own header (None where
-the reference tree is absent, e.g. on the GPU host).  Only tests/,
+the reference tree is absent, e.g. on an aarch64 host).  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU legs use these; the product
 package never imports this module.
 """
