@@ -145,3 +145,44 @@ def test_reference_photographs_decode_like_the_loader(built):
         err, want, rw, rh = oracle.ref_png_decode(data)
         assert err == 0 and (w, h) == (rw, rh), f
         np.testing.assert_array_equal(img, want, err_msg=f)
+
+
+def test_damaged_files_never_crash(built):
+    """Random byte flips, truncations and chunk-length edits of valid files:
+    the decoder returns a decoded image or an error, never reads or writes
+    out of bounds (this test would crash the process), and with the CRCs
+    intact agrees with the loader (lodepng) on whether the file decodes and
+    on the pixels when it does."""
+    rng = np.random.default_rng(99)
+    seeds = []
+    for ctype, depth in ((2, 8), (6, 8), (3, 4), (0, 16), (4, 8)):
+        samples, palette, trns = _case(ctype, depth, 23, 19, ctype * 7 + depth, False)
+        for interlace in (0, 1):
+            seeds.append(write_png(samples, ctype, depth, interlace, palette, trns, idat_split=2))
+    for k in range(400):
+        data = bytearray(seeds[k % len(seeds)])
+        kind = k % 4
+        if kind == 0:  # flip a few payload bytes
+            for _ in range(int(rng.integers(1, 4))):
+                data[int(rng.integers(8, len(data)))] ^= int(rng.integers(1, 256))
+        elif kind == 1:  # truncate
+            data = data[:int(rng.integers(8, len(data)))]
+        elif kind == 2:  # corrupt a chunk length
+            pos = 8 + 4 * int(rng.integers(0, 4))
+            data[pos:pos + 4] = int(rng.integers(0, 2 ** 32)).to_bytes(4, "big")
+        else:  # damage the compressed data and fix the CRC, so only inflate can catch it
+            idat = data.find(b"IDAT")
+            n = int.from_bytes(data[idat - 4:idat], "big")
+            data[idat + 4 + int(rng.integers(0, n))] ^= int(rng.integers(1, 256))
+            crc = zlib.crc32(bytes(data[idat:idat + 4 + n])) & 0xFFFFFFFF
+            data[idat + 4 + n:idat + 8 + n] = crc.to_bytes(4, "big")
+        try:
+            img, w, h = g.read_png(bytes(data), opaque=False)
+            ok = True
+        except ValueError:
+            ok = False
+        if kind == 3 and oracle.load_ref() is not None:
+            err, want, _, _ = oracle.ref_png_decode(bytes(data))
+            assert ok == (err == 0), (k, err)
+            if ok:
+                np.testing.assert_array_equal(img, want)
