@@ -740,13 +740,16 @@ def run_gpu(args):
         quality[names[c]] = {"psnr_rgb_db": round(psnr, 5), "unsupported_blocks": int(sums[4]),
                              "decode_error_kernel_us": round(ms * 1e3, 2),
                              "decode_error_hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
-    mips = run_mips(g, torch, workloads, img, src[0], stream)
-    pair = run_pair(args, g, torch, src, dst, codecs, stream, local)
+    # the per-GPU feature sections run at N = 1 only: with several ranks they
+    # would repeat on every GPU and contend for the shared host cores
+    single = world == 1
+    mips = run_mips(g, torch, workloads, img, src[0], stream) if single else None
+    pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
     batched = None
-    if not args.no_batched:
+    if not args.no_batched and single:
         batched = run_batched(args, g, torch, stream, dev)
     serving = None
-    if not args.no_serving:
+    if not args.no_serving and single:
         serving = run_serving(args, g, local)
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import build as oracle_build
