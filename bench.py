@@ -264,6 +264,41 @@ def run_pair(args, g, torch, src, dst, codecs, stream, device):
             "bit_exact_vs_image_kernels": all(bool(torch.equal(outs[c], dst[c])) for c in codecs)}
 
 
+def run_two_streams(args, g, torch, src, dst, codecs, stream):
+    """The timed step's two launches on two streams at once (the BC1 image
+    on one, the ETC1s image on the other): the bandwidth-bound BC1 kernel and
+    the ALU-bound ETC1s kernel may then share the GPU.  Step time = from the
+    first launch to both finished."""
+    other = torch.cuda.Stream()
+    outs = [torch.empty_like(dst[c]) for c in codecs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_fork, ev_join = torch.cuda.Event(), torch.cuda.Event()
+
+    def step():
+        ev_fork.record(stream)
+        other.wait_event(ev_fork)
+        assert g.compress_device(codecs[1], outs[1].data_ptr(), src[1].data_ptr(), W, H, 4 * W,
+                                 other.cuda_stream) == g.OK
+        assert g.compress_device(codecs[0], outs[0].data_ptr(), src[0].data_ptr(), W, H, 4 * W,
+                                 stream.cuda_stream) == g.OK
+        ev_join.record(other)
+        stream.wait_event(ev_join)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    px = 2 * W * H
+    return {"api": "goofy_gpu_compress_*_device on two streams (ETC1s issued first)", "ms_per_step": round(ms, 4),
+            "mpix_s": round(px / (ms / 1e3) / 1e6, 1), "hbm_gbs": round(ALG_BYTES_PER_PX * px / (ms / 1e3) / 1e9, 1),
+            "bit_exact_vs_image_kernels": all(bool(torch.equal(outs[c], dst[c])) for c in codecs)}
+
+
 def run_mips(g, torch, workloads, img, d_src, stream):
     """Device mip chain of the 8192x8192 image (levels 4096x4096 .. 4x4; up to
     6 levels per launch): median time, HBM rate for the algorithmic bytes (the
@@ -745,6 +780,7 @@ def run_gpu(args):
     single = world == 1
     mips = run_mips(g, torch, workloads, img, src[0], stream) if single else None
     pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
+    two_streams = run_two_streams(args, g, torch, src, dst, codecs, stream) if single else None
     batched = None
     if not args.no_batched and single:
         batched = run_batched(args, g, torch, stream, dev)
@@ -763,7 +799,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
