@@ -73,22 +73,15 @@ __device__ __forceinline__ void store_px(const MipOut& o, int l, uint32_t row, u
     *reinterpret_cast<uint32_t*>(o.data[l] + (size_t)row * o.pitch[l] + 4u * col) = v;
 }
 
-__global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restrict__ src, size_t src_stride,
-                                                        uint32_t tw_log2, uint32_t th_log2, uint32_t nlev, MipOut out)
+// One tile's levels from its thread's 4x4 patch `r` (already loaded).
+__device__ __forceinline__ void mip_tile(const uint4 (&r)[4], bool act, uint32_t tx, uint32_t ty, uint32_t tw_log2,
+                                         uint32_t th_log2, uint32_t nlev, const MipOut& out, uint32_t (*buf)[64])
 {
-    __shared__ uint32_t buf[2][64];
-    const uint32_t tx = blockIdx.x, ty = blockIdx.y, t = threadIdx.x;
-    // second-level tile: (tw/4) x (th/4) pixels, one per thread
+    const uint32_t t = threadIdx.x;
     const uint32_t w2_log2 = tw_log2 - 2, h2_log2 = th_log2 - 2, w2 = 1u << w2_log2;
-    const bool act = t < (1u << (w2_log2 + h2_log2));
     const uint32_t x2 = t & (w2 - 1u), y2 = t >> w2_log2;
     uint32_t v2 = 0;
     if (act) {
-        const uint8_t* patch = src + (((size_t)ty << th_log2) + 4u * y2) * src_stride +
-                               (((size_t)tx << tw_log2) + 4u * x2) * 4u;
-        uint4 r[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) r[k] = __ldg(reinterpret_cast<const uint4*>(patch + (size_t)k * src_stride));
         const uint32_t q00 = box4(r[0].x, r[0].y, r[1].x, r[1].y), q01 = box4(r[0].z, r[0].w, r[1].z, r[1].w);
         const uint32_t q10 = box4(r[2].x, r[2].y, r[3].x, r[3].y), q11 = box4(r[2].z, r[2].w, r[3].z, r[3].w);
         const uint32_t row1 = (ty << (th_log2 - 1)) + 2u * y2, col1 = (tx << (tw_log2 - 1)) + 2u * x2;
@@ -123,6 +116,33 @@ __global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restric
         cw_log2 = nw_log2;
         ch_log2 = nh_log2;
     }
+    __syncthreads();  // the next tile of this CTA reuses buf
+}
+
+// TILES horizontally adjacent tiles per CTA: every patch load of all of them
+// is issued before the first tile is reduced, so more bytes are in flight.
+template <int TILES>
+__global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restrict__ src, size_t src_stride,
+                                                        uint32_t tw_log2, uint32_t th_log2, uint32_t nlev, MipOut out)
+{
+    __shared__ uint32_t buf[2][64];
+    const uint32_t t = threadIdx.x, ty = blockIdx.y;
+    const uint32_t w2_log2 = tw_log2 - 2, h2_log2 = th_log2 - 2, w2 = 1u << w2_log2;
+    const bool act = t < (1u << (w2_log2 + h2_log2));
+    const uint32_t x2 = t & (w2 - 1u), y2 = t >> w2_log2;
+    uint4 r[TILES][4];
+#pragma unroll
+    for (int k = 0; k < TILES; ++k) {
+        if (act) {
+            const uint32_t tx = blockIdx.x * TILES + k;
+            const uint8_t* patch = src + (((size_t)ty << th_log2) + 4u * y2) * src_stride +
+                                   (((size_t)tx << tw_log2) + 4u * x2) * 4u;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r[k][j] = __ldg(reinterpret_cast<const uint4*>(patch + (size_t)j * src_stride));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < TILES; ++k) mip_tile(r[k], act, blockIdx.x * TILES + k, ty, tw_log2, th_log2, nlev, out, buf);
 }
 
 bool pow2(uint32_t v) { return v && !(v & (v - 1)); }
@@ -204,8 +224,13 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
                 mo.data[l] = static_cast<uint8_t*>(levels[i + l].data);
                 mo.pitch[l] = levels[i + l].stride;
             }
-            mip_fused_kernel<<<dim3(up.width / tw, up.height / th), 256, 0, st>>>(
-                static_cast<const uint8_t*>(up.data), up.stride, log2u(tw), log2u(th), f, mo);
+            const uint32_t gx = up.width / tw, gy = up.height / th;
+            if (gx % 2 == 0)  // (two tiles per CTA measured faster than one or four)
+                mip_fused_kernel<2><<<dim3(gx / 2, gy), 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
+                                                                      log2u(tw), log2u(th), f, mo);
+            else
+                mip_fused_kernel<1><<<dim3(gx, gy), 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
+                                                                  log2u(tw), log2u(th), f, mo);
             GOOFY_CUDA_TRY(cudaGetLastError());
             i += f;
             continue;
