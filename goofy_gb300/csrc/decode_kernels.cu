@@ -94,16 +94,34 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
     __shared__ uint32_t pal[8 * 256];
     unsigned long long s[6] = {0, 0, 0, 0, 0, 0};
     const uint32_t bw_magic = 0xffffffffu / bw;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
+    // software pipeline: the next block's source rows and code are loaded
+    // before this block is decoded and compared
+    const uint32_t step = gridDim.x * blockDim.x;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t w[16];
+    uint2 blk = make_uint2(0, 0);
+    if (i < nblk) {
         uint32_t bx;
         const uint32_t by = div_magic(i, bw, bw_magic, bx);
-        uint32_t px[16], w[16];
-        const bool ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), pal + threadIdx.x, blockDim.x, px);
         load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
+        blk = load_block8(blocks + 8u * (size_t)i);
+    }
+    for (; i < nblk; i += step) {
+        uint32_t px[16], cur[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cur[k] = w[k];
+        const uint2 cur_blk = blk;
+        if (i + step < nblk) {
+            uint32_t bx;
+            const uint32_t by = div_magic(i + step, bw, bw_magic, bx);
+            load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
+            blk = load_block8(blocks + 8u * (size_t)(i + step));
+        }
+        const bool ok = decode_block<CODEC>(cur_blk, pal + threadIdx.x, blockDim.x, px);
         uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
-            const uint32_t a[4] = {w[4 * y], w[4 * y + 1], w[4 * y + 2], w[4 * y + 3]};
+            const uint32_t a[4] = {cur[4 * y], cur[4 * y + 1], cur[4 * y + 2], cur[4 * y + 3]};
             const uint32_t b[4] = {px[4 * y], px[4 * y + 1], px[4 * y + 2], px[4 * y + 3]};
             accumulate_row(a, b, acc);
             s[5] += luma_row(a, b);
