@@ -463,9 +463,16 @@ def run_serving(args, g, device):
         tail = lat_ns >= np.percentile(lat_ns, 99)
         sub, adm, lau, done = (stamps[tail, k].astype(np.float64) for k in range(4))
         sched = done - lat_ns[tail]
-        return {k: round(float(v.mean()) / 1e6, 3) for k, v in
-                (("submit_late", sub - sched), ("queued", adm - sub), ("admitted", lau - adm),
-                 ("launch_to_done", done - lau))}
+        out = {k: round(float(v.mean()) / 1e6, 3) for k, v in
+               (("submit_late", sub - sched), ("queued", adm - sub), ("admitted", lau - adm),
+                ("launch_to_done", done - lau))}
+        w = int(np.argmax(lat_ns))  # and the single slowest request
+        st = stamps[w].astype(np.float64)
+        ws = st[3] - lat_ns[w]
+        out["slowest"] = {k: round(float(v) / 1e6, 3) for k, v in
+                          (("submit_late", st[0] - ws), ("queued", st[1] - st[0]), ("admitted", st[2] - st[1]),
+                           ("launch_to_done", st[3] - st[2]))}
+        return out
 
     def classes(px, probe, lat_ns):
         out = {}
