@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=4.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
-    p.add_argument("--profile", choices=["encode", "quality", "mips"],
+    p.add_argument("--profile", choices=["encode", "quality", "mips", "batch"],
                    help="only run a few launches of one kernel family (for ncu captures) and exit")
     p.add_argument("--profile-size", type=int, default=4096, help="image side for --profile")
     return p.parse_args()
@@ -830,6 +830,25 @@ def run_profile(args):
 
     lib_build.build()
     assert g.init(0) == g.OK, g.last_error()
+    if args.profile == "batch":  # the mixed batch of --batch-textures textures, three launches, default tile
+        levels = workloads.texture_batch(args.batch_textures)
+        keep, descs = [], []
+        for lv in levels:
+            src = torch.from_numpy(np.ascontiguousarray(lv["pixels"]).reshape(-1)).cuda()
+            out = torch.empty(g.out_size(lv["width"], lv["height"]), dtype=torch.uint8, device="cuda")
+            keep += [src, out]
+            descs.append((src.data_ptr(), out.data_ptr(), lv["width"], lv["height"], lv["pixels"].strides[0],
+                          lv["codec"]))
+        b = g.Batch(len(descs))
+        try:
+            arr = g.images_array(descs)
+            for _ in range(3):
+                assert b.encode(arr, torch.cuda.current_stream().cuda_stream) == g.OK, g.last_error()
+            torch.cuda.synchronize()
+        finally:
+            b.close()
+        print(json.dumps({"profile": "batch", "textures": args.batch_textures, "levels": len(descs)}))
+        return 0
     n = args.profile_size
     img = workloads.scene(n, n, SEED, n // 256, max(8, n * n // 32768), threads=0)
     src = torch.from_numpy(img.reshape(-1)).cuda()
