@@ -161,8 +161,8 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
 #pragma unroll
     for (int y = 0; y < 4; ++y)
 #pragma unroll
-        for (int x = 0; x < 2; ++x)  // lanes G(y, x), G(y, x+2)
-            gp[2 * y + x] = perm(w[4 * y + x], w[4 * y + x + 2], 0x0501u) & 0x00ff00ffu;
+        for (int x = 0; x < 2; ++x)  // lanes G(y, x), G(y, x+2): byte dot products and a multiply-add (FMA pipe)
+            gp[2 * y + x] = __dp4a(w[4 * y + x + 2], 0x00000100u, 0u) * 0x10000u + __dp4a(w[4 * y + x], 0x00000100u, 0u);
     const uint32_t mn_rb = tree_min<16>(rb), mx_rb = tree_max<16>(rb);
     uint32_t mn_g = tree_min<8>(gp), mx_g = tree_max<8>(gp);
     mn_g = vmin2(mn_g, mn_g >> 16);
