@@ -60,6 +60,10 @@ GOOFY_FN uint32_t luma_sum(uint32_t px, uint32_t acc) { return __dp4a(px, 0x0001
 // Y = avg(avg(R,B),G) of an RGB word
 GOOFY_FN uint32_t luma(uint32_t px) { return luma_sum(px, 3u) >> 2; }
 
+// The same from an R/B lane word (R in byte 0, B in byte 2) and a word with G
+// in byte 0: two byte dot products, no repacking.
+GOOFY_FN uint32_t luma_lanes(uint32_t rb, uint32_t g) { return __dp4a(rb, 0x00010001u, __dp4a(g, 0x00000002u, 3u)) >> 2; }
+
 // to5 on both 16-bit lanes
 GOOFY_FN uint32_t to5x2(uint32_t lanes) { return ((vmax2(lanes, 0x00010001u) - 0x00010001u) >> 3) & 0x001f001fu; }
 
@@ -96,11 +100,11 @@ struct BlockRange {
     uint32_t range, mid, qt;
 };
 
-// Brightness statistics of the block from its channel min / max words
-// (bytes R,G,B,x), goofy_tc.h:1151-1190.
-GOOFY_FN BlockRange block_range(uint32_t mn_rgb, uint32_t mx_rgb)
+// Brightness statistics of the block from its channel min / max (R/B lane
+// words and G in byte 0), goofy_tc.h:1151-1190.
+GOOFY_FN BlockRange block_range(uint32_t mn_rb, uint32_t mn_g, uint32_t mx_rb, uint32_t mx_g)
 {
-    const uint32_t ymin = luma(mn_rgb), ymax = luma(mx_rgb);
+    const uint32_t ymin = luma_lanes(mn_rb, mn_g), ymax = luma_lanes(mx_rb, mx_g);
     BlockRange r;
     r.range = max(ymax - ymin, 8u);
     r.mid = (ymin + ymax + 1u) >> 1;
@@ -124,7 +128,7 @@ GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
     uint32_t mn_g = tree_min<8>(gg), mx_g = tree_max<8>(gg);
     mn_g = vmin2(mn_g, mn_g >> 16);  // byte 0 = min G
     mx_g = vmax2(mx_g, mx_g >> 16);
-    const BlockRange br = block_range(perm(mn_rb, mn_g, 0x1240u), perm(mx_rb, mx_g, 0x1240u));
+    const BlockRange br = block_range(mn_rb, mn_g, mx_rb, mx_g);
 
     // thresholds on S of two pixels at once (16-bit lanes): flag bits 14 / 15
     const uint32_t k_gez = (0x4003u - 4u * br.mid) * 0x10001u;                // bit 14: Y >= mid
@@ -167,7 +171,7 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     uint32_t mn_g = tree_min<8>(gp), mx_g = tree_max<8>(gp);
     mn_g = vmin2(mn_g, mn_g >> 16);
     mx_g = vmax2(mx_g, mx_g >> 16);
-    const BlockRange br = block_range(perm(mn_rb, mn_g, 0x1240u), perm(mx_rb, mx_g, 0x1240u));
+    const BlockRange br = block_range(mn_rb, mn_g, mx_rb, mx_g);
 
     // block mean, rounding-average tree kept exact at scale 2^level
     uint32_t col_rb[4];
@@ -191,7 +195,7 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     const uint32_t m_g = ((uv_g + (uv_g >> 16) + 8u) & 0xfff0u) >> 4;
 
     // move the mean's brightness onto mid, goofy_tc.h:1416-1449
-    const uint32_t ya = luma(perm(m_rb, m_g, 0x1240u));
+    const uint32_t ya = luma_lanes(m_rb, m_g);
     const bool up = ya <= br.mid;
     const uint32_t corr = min(up ? br.mid - ya : ya - br.mid, 0x7fu);
     const uint32_t corr2 = corr * 0x00010001u;
