@@ -145,6 +145,8 @@ def _declare(lib):
         "goofy_gpu_mip_arena_bytes": (ctypes.c_size_t, [_U32, _U32]),
         "goofy_gpu_generate_mips": (ctypes.c_int, [_VP, _U32, _U32, _U32, _VP, ctypes.c_size_t, ctypes.POINTER(Level),
                                                    _U32, ctypes.POINTER(_U32), _VP]),
+        "goofy_gpu_tga_size": (ctypes.c_size_t, [_U32, _U32]),
+        "goofy_gpu_write_tga": (ctypes.c_int, [_VP, _U32, _U32, _U32, _VP, ctypes.c_size_t]),
         "goofy_gpu_container_size": (ctypes.c_size_t, [ctypes.c_int, _VP, _VP, _U32]),
         "goofy_gpu_write_container": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _VP, _U32, _VP, ctypes.c_size_t]),
         "goofy_gpu_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
@@ -558,3 +560,18 @@ def read_png(source, opaque=True, stride=None):
     if rc != OK:
         raise ValueError("png: %s %s" % (status_string(rc), last_error()))
     return img, w.value, h.value
+
+
+def tga(rgba, width, height):
+    """The harness's TGA file bytes (saveTga) of a host RGBA8 image (rows of its stride)."""
+    import numpy as np
+
+    img = np.ascontiguousarray(rgba)
+    n = lib().goofy_gpu_tga_size(width, height)
+    if n == 0:
+        raise ValueError("tga: unsupported size %dx%d" % (width, height))
+    out = np.zeros(n, np.uint8)
+    rc = lib().goofy_gpu_write_tga(img.ctypes.data, img.strides[0], width, height, out.ctypes.data, n)
+    if rc != OK:
+        raise RuntimeError("tga: %s %s" % (status_string(rc), last_error()))
+    return out.tobytes()

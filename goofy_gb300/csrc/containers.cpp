@@ -4,7 +4,10 @@
 // same bytes, including the reference's header field choices (DDS flags
 // 0x000A1007, caps left 0; KTX glTypeSize 1, GL_RGB base format).  More than
 // one level (a mip chain) sets the level count and appends the levels in
-// order, each KTX level preceded by its byte size.
+// order, each KTX level preceded by its byte size.  The harness's TGA images
+// (saveTga, Src/main.cpp:222-255: an 18-byte header, type 2, 32 bits per
+// pixel, top-left origin, then BGRA pixels) hold its original, baseline and
+// decoded images.
 #include <cstring>
 
 #include "../../include/goofy_gpu.h"
@@ -87,6 +90,39 @@ GOOFY_EXPORT int goofy_gpu_write_container(int codec, const uint8_t* const* leve
             p += 4;
             if (n) std::memcpy(p, level_blocks[i], n);
             p += n;  // n is a multiple of 8: no mip padding
+        }
+    }
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT size_t goofy_gpu_tga_size(uint32_t width, uint32_t height)
+{
+    if (width == 0 || height == 0 || width > 65535 || height > 65535) return 0;
+    return 18 + (size_t)width * height * 4;
+}
+
+GOOFY_EXPORT int goofy_gpu_write_tga(const uint8_t* rgba, uint32_t stride, uint32_t width, uint32_t height,
+                                     uint8_t* out, size_t out_size)
+{
+    const size_t need = goofy_gpu_tga_size(width, height);
+    if (need == 0 || !rgba || !out || (uint64_t)stride < 4ull * width) return GOOFY_ERR_INVALID;
+    if (out_size < need) return goofy_gpu::fail(GOOFY_ERR_TOO_LARGE, "tga: output buffer too small");
+    std::memset(out, 0, 18);
+    out[2] = 2;  // uncompressed true colour
+    out[12] = (uint8_t)width;
+    out[13] = (uint8_t)(width >> 8);
+    out[14] = (uint8_t)height;
+    out[15] = (uint8_t)(height >> 8);
+    out[16] = 32;    // bits per pixel
+    out[17] = 0x20;  // rows stored top first
+    uint8_t* p = out + 18;
+    for (uint32_t y = 0; y < height; ++y) {
+        const uint8_t* row = rgba + (size_t)y * stride;
+        for (uint32_t x = 0; x < width; ++x, p += 4) {
+            p[0] = row[4 * x + 2];
+            p[1] = row[4 * x + 1];
+            p[2] = row[4 * x + 0];
+            p[3] = row[4 * x + 3];
         }
     }
     return GOOFY_OK;

@@ -8,8 +8,10 @@
       time them, :646-664), measured with the harness's getMsePsnr record
       (on the GPU) and printed as the harness's result rows
       (Image;Encoder;Format;NumberOfPixels;time (us);MP/s;mse...;psnr...;delta...),
-      deltas against its RGB565 downsample baseline row.  With --out the
-      blocks are written as DDS / KTX files as the harness writes them.
+      deltas against its RGB565 downsample baseline row.  With --out it
+      writes the files the harness writes: DDS / KTX blocks, the decoded
+      images (decoded on the GPU) and the original and baseline images as
+      TGA.
 
   python -m goofy_gb300.tool encode IN.png OUT.dds|OUT.ktx [--codec bc1|etc1s] [--mips]
       One PNG to a DDS (BC1) or KTX (ETC1s) file, optionally with a full mip
@@ -86,6 +88,11 @@ def result_row(image, encoder, fmt, pixels, time_us, q, base):
     return ";".join([image, encoder, fmt, "%3.0f" % pixels, "%3.0f" % time_us, "%3.5f" % mps] + fields + deltas)
 
 
+def write(folder, name, data):
+    with open(os.path.join(folder, name), "wb") as f:
+        f.write(data)
+
+
 def run_image(path, iterations, out_dir, torch):
     """Result rows for one photograph (baseline, ETC1, DXT1), or None when
     the harness would refuse it (width % 16, height % 4)."""
@@ -94,11 +101,15 @@ def run_image(path, iterations, out_dir, torch):
     if w % 16 or h % 4:
         print("%s: %dx%d refused (width must be a multiple of 16, height of 4)" % (name, w, h), file=sys.stderr)
         return None
-    base = mse_psnr_images(img, baseline_rgb565(img, w, h), w, h)
+    base_img = baseline_rgb565(img, w, h)
+    base = mse_psnr_images(img, base_img, w, h)
     rows = [result_row(name, "Baseline (Downsample x2)", "RGB565", w * h, 0, base, base)]
     d_src = torch.from_numpy(img.reshape(-1)).cuda()
-    for codec, fmt, fn, ext in ((g.CODEC_ETC1S, "ETC1", g.compressETC1, "etc1.ktx"),
-                                (g.CODEC_BC1, "DXT1", g.compressDXT1, "dxt1.dds")):
+    if out_dir:
+        write(out_dir, name + "_original.tga", g.tga(img, w, h))
+        write(out_dir, name + "_baseline.tga", g.tga(base_img, w, h))
+    for codec, fmt, fn, kind, ext in ((g.CODEC_ETC1S, "ETC1", g.compressETC1, "etc1", "ktx"),
+                                      (g.CODEC_BC1, "DXT1", g.compressDXT1, "dxt1", "dds")):
         out = np.zeros(g.out_size(w, h), np.uint8)
         best = float("inf")
         for _ in range(iterations):
@@ -107,11 +118,17 @@ def run_image(path, iterations, out_dir, torch):
             best = min(best, (time.perf_counter() - t0) * 1e6)
             if rc != 0:
                 raise RuntimeError("%s: encode failed %d %s" % (name, rc, g.last_error()))
-        q = g.mse_psnr(codec, torch.from_numpy(out).cuda(), d_src, w, h, 4 * w)
+        d_blocks = torch.from_numpy(out).cuda()
+        q = g.mse_psnr(codec, d_blocks, d_src, w, h, 4 * w)
         rows.append(result_row(name, ENCODER, fmt, w * h, best, q, base))
         if out_dir:
-            with open(os.path.join(out_dir, "%s_%s_%s" % (name, ENCODER, ext)), "wb") as f:
-                f.write(g.container(codec, [(out, w, h)]))
+            stem = "%s_%s_%s" % (name, ENCODER, kind)
+            write(out_dir, stem + "." + ext, g.container(codec, [(out, w, h)]))
+            rgba = torch.empty(4 * w * h, dtype=torch.uint8, device="cuda")
+            bad = torch.zeros(1, dtype=torch.int64, device="cuda")
+            assert g.decode_device(codec, rgba, 4 * w, d_blocks, w, h, bad) == g.OK, g.last_error()
+            torch.cuda.synchronize()
+            write(out_dir, stem + "_decompressed.tga", g.tga(rgba.cpu().numpy().reshape(h, 4 * w), w, h))
     return rows
 
 

@@ -228,6 +228,13 @@ size_t goofy_gpu_container_size(int codec, const uint32_t* widths, const uint32_
 int goofy_gpu_write_container(int codec, const uint8_t* const* level_blocks, const uint32_t* widths,
                               const uint32_t* heights, uint32_t levels, uint8_t* out, size_t out_size);
 
+/* The harness's TGA image (saveTga, Src/main.cpp:222-255): an 18-byte header
+ * (type 2, 32 bits per pixel, top-left origin) and BGRA pixels, from RGBA8
+ * rows.  goofy_gpu_tga_size is 0 for sizes TGA cannot hold (above 65535). */
+size_t goofy_gpu_tga_size(uint32_t width, uint32_t height);
+int goofy_gpu_write_tga(const uint8_t* rgba, uint32_t stride, uint32_t width, uint32_t height, uint8_t* out,
+                        size_t out_size);
+
 /* ---- batches: many device images of uneven sizes in one launch ----------- */
 
 /* One image of a batch (a texture or one of its mip levels).  src / dst and

@@ -14,7 +14,9 @@ For every PNG in the reference's test-data/ that its harness accepts
   Src/decoder.cpp and to the harness run below);
 * the harness's own result rows (Goofy and its RGB565 baseline) for its
   default image (parrot_red), from one run of the harness compiled from the
-  reference tree (oracle/run_harness.py), as printed (5 decimals).
+  reference tree (oracle/run_harness.py), as printed (5 decimals), and the
+  SHA-256 of the files that run wrote for Goofy (DDS, KTX, the decoded TGA
+  images) and of its original and baseline TGA images.
 
 Run:  python tests/golden/make_photo_digests.py
 """
@@ -62,8 +64,14 @@ def main():
                             "mse_psnr": oracle.mse_psnr(img, dec, w, h)}
         photos[name] = entry
     harness = [r for r in run_harness.run() if r["encoder"] in ("simd_goofy", "Baseline (Downsample x2)")]
+    files = {}
+    for suffix in ("original.tga", "baseline.tga", "simd_goofy_dxt1.dds", "simd_goofy_dxt1_decompressed.tga",
+                   "simd_goofy_etc1.ktx", "simd_goofy_etc1_decompressed.tga"):
+        name = "parrot_red_" + suffix
+        with open(os.path.join(run_harness.RUN_DIR, "test-results", name), "rb") as f:
+            files[name] = hashlib.sha256(f.read()).hexdigest()
     with open(OUT, "w") as f:
-        json.dump({"photos": photos, "harness_rows": harness}, f, indent=1, sort_keys=True)
+        json.dump({"photos": photos, "harness_rows": harness, "harness_files": files}, f, indent=1, sort_keys=True)
     print("wrote", OUT, len(photos), "photos,", len(harness), "harness rows")
 
 

@@ -65,3 +65,20 @@ def test_all_photographs_in_one_batch(cuda):
         b.close()
     for s, o, w, h, c, want in items:
         assert _sha(o.cpu().numpy()) == want
+
+
+@needs_photos
+def test_tool_writes_the_harness_files(cuda, tmp_path):
+    """`tool run --out` on parrot_red writes the harness's files byte for byte:
+    DDS / KTX, the GPU-decoded TGA images, the original and the baseline."""
+    import contextlib
+    import io
+
+    from goofy_gb300 import tool
+
+    with contextlib.redirect_stdout(io.StringIO()):
+        assert tool.main(["run", "--data", TEST_DATA, "--images", "parrot_red", "--iterations", "2",
+                          "--out", str(tmp_path)]) == 0
+    got = {p.name.replace(tool.ENCODER, "simd_goofy"): hashlib.sha256(p.read_bytes()).hexdigest()
+           for p in tmp_path.iterdir()}
+    assert got == DIGESTS["harness_files"]

@@ -51,5 +51,6 @@ def test_run_prints_harness_rows(cuda, tmp_path):
     assert [r[:3] for r in rows] == [["a", "Baseline (Downsample x2)", "RGB565"], ["a", tool.ENCODER, "ETC1"],
                                      ["a", tool.ENCODER, "DXT1"]]
     assert all(len(r) == 21 for r in rows)
-    assert sorted(p.name for p in (tmp_path / "out").iterdir()) == ["a_gb300_goofy_dxt1.dds",
-                                                                   "a_gb300_goofy_etc1.ktx"]
+    assert sorted(p.name for p in (tmp_path / "out").iterdir()) == [
+        "a_baseline.tga", "a_gb300_goofy_dxt1.dds", "a_gb300_goofy_dxt1_decompressed.tga", "a_gb300_goofy_etc1.ktx",
+        "a_gb300_goofy_etc1_decompressed.tga", "a_original.tga"]

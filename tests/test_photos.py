@@ -88,3 +88,23 @@ def test_tool_rows_match_the_harness_rows(built):
         for k in HARNESS_FIELDS:
             if k != "mps":  # the harness divides its rounded-to-print time; mps follows from time_us
                 assert got[k] == want[k], (fmt, k)
+
+
+@pytest.mark.skipif(not os.path.isdir(TEST_DATA), reason="reference test photographs not present")
+def test_harness_files_byte_for_byte(built):
+    """The files the harness wrote for parrot_red -- DDS, KTX, decoded TGA
+    images, the original and the RGB565 baseline -- equal, byte for byte, the
+    library's container / TGA writers fed with the oracle's blocks and decode
+    and the command-line tool's baseline."""
+    from goofy_gb300 import tool
+
+    want = DIGESTS["harness_files"]
+    img, w, h = g.read_png(os.path.join(TEST_DATA, "parrot_red.png"))
+    got = {"parrot_red_original.tga": g.tga(img, w, h),
+           "parrot_red_baseline.tga": g.tga(tool.baseline_rgb565(img, w, h), w, h)}
+    for codec, kind, ext in ((0, "dxt1", "dds"), (1, "etc1", "ktx")):
+        blocks = oracle.encode(codec, img, w, h, any_width=False)
+        dec, _ = oracle.decode(codec, blocks, w, h)
+        got["parrot_red_simd_goofy_%s.%s" % (kind, ext)] = g.container(codec, [(blocks, w, h)])
+        got["parrot_red_simd_goofy_%s_decompressed.tga" % kind] = g.tga(dec, w, h)
+    assert {k: hashlib.sha256(v).hexdigest() for k, v in got.items()} == want
