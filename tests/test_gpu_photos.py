@@ -24,6 +24,13 @@ def _sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+def _names():
+    """The digested photographs present in the folder (all of them in a full run)."""
+    names = [n for n in sorted(DIGESTS["photos"]) if os.path.exists(os.path.join(TEST_DATA, n + ".png"))]
+    assert names, "no digested photograph in " + TEST_DATA
+    return names
+
+
 def _load(name):
     d = DIGESTS["photos"][name]
     img, w, h = g.read_png(os.path.join(TEST_DATA, name + ".png"))
@@ -33,7 +40,7 @@ def _load(name):
 
 @needs_photos
 def test_photographs_dropin_and_quality(cuda):
-    for name in sorted(DIGESTS["photos"]):
+    for name in _names():
         d, img, w, h = _load(name)
         d_src = cuda.from_numpy(img.reshape(-1)).cuda()
         for codec, (cname, fn) in enumerate((("bc1", g.compressDXT1), ("etc1s", g.compressETC1))):
@@ -51,7 +58,7 @@ def test_photographs_dropin_and_quality(cuda):
 @needs_photos
 def test_all_photographs_in_one_batch(cuda):
     items = []
-    for name in sorted(DIGESTS["photos"]):
+    for name in _names():
         d, img, w, h = _load(name)
         src = cuda.from_numpy(img.reshape(-1)).cuda()
         for codec, cname in enumerate(("bc1", "etc1s")):
