@@ -122,16 +122,23 @@ GOOFY_FN bool decode_block(uint2 blk, uint32_t* store, uint32_t stride, uint32_t
         // the block is big-endian: bytes 0..3 of blk.x are bits 63..32
         const uint32_t w0 = perm(blk.x, 0u, 0x0123u), w1 = perm(blk.y, 0u, 0x0123u);
         const bool flip = w0 & 1u;
-        uint32_t b0, b1, pal[8];
+        uint32_t b0, b1, pal[4];
         const bool ok = etc1_bases(w0, b0, b1);
+        // ETC1s blocks (zero deltas, one table) have one palette for both
+        // sub-blocks: it is built and stored once
+        const bool one = b0 == b1 && ((w0 >> 5) & 7u) == ((w0 >> 2) & 7u);
         etc1_subpalette(b0, (w0 >> 5) & 7u, pal);
-        etc1_subpalette(b1, (w0 >> 2) & 7u, pal + 4);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) store[k * stride] = ok ? pal[k] : 0u;
+        for (int k = 0; k < 4; ++k) store[k * stride] = ok ? pal[k] : 0u;
+        if (!one) {
+            etc1_subpalette(b1, (w0 >> 2) & 7u, pal);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) store[(4 + k) * stride] = ok ? pal[k] : 0u;
+        }
         const uint32_t codes = etc1_codes(w1);
         // sub-block 1: right half (x >= 2) without flip, bottom half (y >= 2) with flip
-        const uint32_t lower_right = 4u * stride, upper_right = flip ? 0u : 4u * stride,
-                       lower_left = flip ? 4u * stride : 0u;
+        const uint32_t s1 = one ? 0u : 4u * stride;
+        const uint32_t lower_right = s1, upper_right = flip ? 0u : s1, lower_left = flip ? s1 : 0u;
 #pragma unroll
         for (int y = 0; y < 4; ++y)
 #pragma unroll
