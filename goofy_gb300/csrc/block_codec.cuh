@@ -67,25 +67,33 @@ GOOFY_FN uint32_t luma_lanes(uint32_t rb, uint32_t g) { return __dp4a(rb, 0x0001
 // to5 on both 16-bit lanes
 GOOFY_FN uint32_t to5x2(uint32_t lanes) { return ((vmax2(lanes, 0x00010001u) - 0x00010001u) >> 3) & 0x001f001fu; }
 
-// Lane-wise min / max of N words as a tree of three-input steps, min(min(a, b), c),
-// which the compiler issues as single three-input lane min / max instructions.
-template <int N>
-GOOFY_FN uint32_t tree_min(const uint32_t* v)
+// Lane-wise min / max of N words, reduced three words at a time
+// (min(min(a, b), c) is one three-input lane min / max instruction): 16 words
+// take 8 instructions, 8 words 4.
+template <int N, bool MAX>
+GOOFY_FN uint32_t tree_reduce(const uint32_t* v)
 {
     if constexpr (N == 1) return v[0];
-    else if constexpr (N == 2) return vmin2(v[0], v[1]);
-    else if constexpr (N == 3) return vmin2(vmin2(v[0], v[1]), v[2]);
-    else return vmin2(vmin2(tree_min<N / 3>(v), tree_min<N / 3>(v + N / 3)), tree_min<N - 2 * (N / 3)>(v + 2 * (N / 3)));
+    else if constexpr (N == 2) return MAX ? vmax2(v[0], v[1]) : vmin2(v[0], v[1]);
+    else {
+        constexpr int M = (N + 2) / 3;
+        uint32_t r[M];
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            const int n = N - 3 * i < 3 ? N - 3 * i : 3;
+            const uint32_t* p = v + 3 * i;
+            r[i] = n == 1 ? p[0] : n == 2 ? (MAX ? vmax2(p[0], p[1]) : vmin2(p[0], p[1]))
+                                          : (MAX ? vmax2(vmax2(p[0], p[1]), p[2]) : vmin2(vmin2(p[0], p[1]), p[2]));
+        }
+        return tree_reduce<M, MAX>(r);
+    }
 }
 
 template <int N>
-GOOFY_FN uint32_t tree_max(const uint32_t* v)
-{
-    if constexpr (N == 1) return v[0];
-    else if constexpr (N == 2) return vmax2(v[0], v[1]);
-    else if constexpr (N == 3) return vmax2(vmax2(v[0], v[1]), v[2]);
-    else return vmax2(vmax2(tree_max<N / 3>(v), tree_max<N / 3>(v + N / 3)), tree_max<N - 2 * (N / 3)>(v + 2 * (N / 3)));
-}
+GOOFY_FN uint32_t tree_min(const uint32_t* v) { return tree_reduce<N, false>(v); }
+
+template <int N>
+GOOFY_FN uint32_t tree_max(const uint32_t* v) { return tree_reduce<N, true>(v); }
 
 // Run starts of etc1BrighnessRangeTocontrolByte (goofy_tc.h:1040-1057); all
 // are even, so a 128-entry table indexed by range>>1 reproduces it.
@@ -108,7 +116,7 @@ GOOFY_FN BlockRange block_range(uint32_t mn_rb, uint32_t mn_g, uint32_t mx_rb, u
     BlockRange r;
     r.range = max(ymax - ymin, 8u);
     r.mid = (ymin + ymax + 1u) >> 1;
-    const uint32_t quarter = (((r.range + 1u) >> 1) + 1u) >> 1;
+    const uint32_t quarter = (r.range + 3u) >> 2;  // avg(avg(range, 0), 0)
     r.qt = quarter + ((quarter + 1u) >> 1);
     return r;
 }
@@ -183,7 +191,8 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     }
     const uint32_t u_rb = (col_rb[0] + col_rb[1] + 0x00040004u) & 0xfff8fff8u;
     const uint32_t v_rb = (col_rb[2] + col_rb[3] + 0x00040004u) & 0xfff8fff8u;
-    const uint32_t m_rb = ((u_rb + v_rb + 0x00080008u) & 0xfff0fff0u) >> 4;  // lanes mean R, mean B
+    // last level with a bias of 256 (0x1000 before the shift): lanes 256 + mean R, 256 + mean B
+    const uint32_t m_rb = ((u_rb + v_rb + 0x10081008u) & 0xfff0fff0u) >> 4;
     uint32_t col_g[2];
 #pragma unroll
     for (int x = 0; x < 2; ++x) {
@@ -192,18 +201,26 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
         col_g[x] = (a + b + 0x00020002u) & 0xfffcfffcu;  // lanes 4*col(x), 4*col(x+2)
     }
     const uint32_t uv_g = (col_g[0] + col_g[1] + 0x00040004u) & 0xfff8fff8u;
-    const uint32_t m_g = ((uv_g + (uv_g >> 16) + 8u) & 0xfff0u) >> 4;
+    const uint32_t m_g = ((uv_g + (uv_g >> 16) + 0x1008u) & 0xfff0u) >> 4;  // 256 + mean G
 
-    // move the mean's brightness onto mid, goofy_tc.h:1416-1449
-    const uint32_t ya = luma_lanes(m_rb, m_g);
-    const bool up = ya <= br.mid;
-    const uint32_t corr = min(up ? br.mid - ya : ya - br.mid, 0x7fu);
-    const uint32_t corr2 = corr * 0x00010001u;
-    const uint32_t base_rb = up ? vmin2(m_rb + corr2, 0x00ff00ffu) : vmax2(m_rb, corr2) - corr2;
-    const uint32_t base_g = up ? min(m_g + corr, 0xffu) : max(m_g, corr) - corr;
-    const uint32_t rb5 = to5x2(base_rb);
-    const uint32_t g5 = to5x2(base_g);
-    const uint32_t word0 = (uint32_t)ctrl_lut[br.range >> 1] << 24 | rb5 << 3 | g5 << 11;
+    // Move the mean's brightness onto mid (goofy_tc.h:1416-1449): with
+    // corr = min(|mid - Y(mean)|, 127) the base is min(mean + corr, 255) when
+    // Y(mean) <= mid and max(mean - corr, 0) otherwise, i.e.
+    //     base = clamp(mean + d, 0, 255),   d = mid - Y(mean),
+    // the clamp of corr to 127 never acting: every channel of the mean lies in
+    // [(max + 15 min) / 16, (15 max + min) / 16 + 2] (one bright pixel moves it
+    // by at least a sixteenth; each level of rounding averages adds at most
+    // 1/2), which keeps Y(mean) within 7/16 * 255 + 3 < 115 of mid.  Then
+    // to5(base) = (clamp(mean + d, 1, 255) - 1) >> 3.  On the biased lanes
+    // (the bias sits in bytes 1 / 3, which the luma dot products skip) that is
+    // (clamp(lane + d, 257, 511) - 257) >> 3, so to5(base) << 3 is
+    // (clamp(lane + d, 257, 511) - 257) & 0xf8, one mask for R, G and B
+    // together once the three clamped lanes minus 257 sit in bytes 0, 1, 2.
+    const int d = (int)br.mid - (int)luma_lanes(m_rb, m_g);
+    const uint32_t c_rb = vmin2(vmax2(m_rb + (uint32_t)d * 0x00010001u, 0x01010101u), 0x01ff01ffu);
+    const uint32_t c_g = min(max(m_g + (uint32_t)d, 257u), 511u);
+    const uint32_t rgb = c_rb + c_g * 256u - 257u * 0x00010101u;  // bytes 0, 1, 2: clamped R, G, B - 257
+    const uint32_t word0 = (uint32_t)ctrl_lut[br.range >> 1] << 24 | (rgb & 0x00f8f8f8u);
 
     // indices: bit j = not gez, bit 16+j = not lqt of the pixel with
     // j = 4*(x^2) + y (transposeAs4x4x4 order, goofy_tc.h:1366-1395).
@@ -213,13 +230,13 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
     // separates them from their final bit: j = 11..15 (m = j-11, no shift),
     // j = 6..10 (m = j-6, >> 5), j = 1..5 (m = j-1, >> 10), j = 0 (>> 11);
     // flags within a group are distinct bits, so groups are summed and
-    // shifted once.  Thresholds are clamped to [0, 1021], which keeps every
-    // lane value in [0, 4096) * 2^m without changing a test.
-    const uint32_t t_gez = min(max(4 * (int)br.mid - 3, 0), 1021);
-    const uint32_t t_lo = min(max(4 * ((int)br.mid - (int)br.qt) + 1, 0), 1021);
-    const uint32_t t_hi = min(4u * (br.mid + br.qt) - 3u, 1021u);
-    const uint32_t k_q = (2048u - t_gez) | (2048u - t_lo) << 16;
-    const uint32_t k_h = (2048u - t_hi) << 16;  // h: low lane S, high lane S + 2048 - t_hi
+    // shifted once.  A test S >= t is bit 11 of S + 2048 - t; with S <= 1020,
+    // mid <= 255 and qt <= 96 the thresholds t_gez = 4 mid - 3,
+    // t_lo = 4 (mid - qt) + 1 and t_hi = 4 (mid + qt) - 3 keep every lane
+    // value in [0, 4096), so bit 11 is the test and the lanes, even scaled by
+    // 2^4, never carry into each other.
+    const uint32_t k_q = 0x07ff0803u + br.qt * 0x00040000u - br.mid * 0x00040004u;  // 2048 - t_gez | 2048 - t_lo
+    const uint32_t k_h = (0x0803u - 4u * (br.mid + br.qt)) << 16;                    // h: S | S + 2048 - t_hi
     uint32_t group[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int y = 0; y < 4; ++y)
@@ -230,7 +247,7 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
             const int m = j >= 11 ? j - 11 : j >= 6 ? j - 6 : j >= 1 ? j - 1 : 0;
             const uint32_t s = luma_sum(w[4 * y + x], 0u);
             const uint32_t q = s * (0x00010001u << m) + (k_q << m);  // bit 11+m: Y >= mid, 27+m: Y >= mid-qt+1
-            const uint32_t h = s * (0x00010001u << m) + (k_h << m);  // bit 27+m: Y >= mid+qt; bit 11+m clear
+            const uint32_t h = q + ((k_h - k_q) << m);                // bit 27+m: Y >= mid+qt; bit 11+m clear
             group[gi] += (~q | h) & (0x08000800u << m);
         }
     const uint32_t word1 = group[0] + (group[1] >> 5) + (group[2] >> 10) + (group[3] >> 11);

@@ -41,6 +41,35 @@ def test_random_vs_oracle(emu, seed):
         np.testing.assert_array_equal(_encode(emu, codec, img, w, h), oracle.encode(codec, img, w, h))
 
 
+def test_edge_blocks_vs_oracle(emu):
+    """Blocks whose channel bounds sit at or next to 0, 127/128 and 255: the
+    brightness mid and the thresholds reach the ends of their ranges (mid 0 /
+    255, qt 96, a mean pushed past 0 or 255 by the correction)."""
+    rng = np.random.default_rng(5)
+    w, h = 1024, 256
+    edges = np.array([0, 1, 2, 3, 8, 120, 127, 128, 135, 247, 252, 253, 254, 255])
+    n = (h // 4) * (w // 4)
+    lo = edges[rng.integers(0, len(edges), (n, 1, 4))]
+    hi = edges[rng.integers(0, len(edges), (n, 1, 4))]
+    lo, hi = np.minimum(lo, hi), np.maximum(lo, hi)
+    # per pixel: one of the bounds (most), or a value between them
+    pick = rng.integers(0, 3, (n, 16, 4))
+    mid = lo + ((hi - lo + 1) * rng.random((n, 16, 4))).astype(np.int64)
+    px = np.where(pick == 0, lo, np.where(pick == 1, hi, np.minimum(mid, hi)))
+    # a quarter of the blocks: all pixels at one bound but one at the other,
+    # which pulls the mean farthest from the brightness mid
+    odd = rng.integers(0, 16, n)
+    one = np.arange(16)[None, :] == odd[:, None]
+    first = rng.integers(0, 2, n).astype(bool)[:, None, None]
+    lone = np.where(one[:, :, None], np.where(first, hi, lo), np.where(first, lo, hi))
+    sel = (np.arange(n) % 4 == 0)[:, None, None]
+    px = np.where(sel, lone, px)
+    img = px.reshape(h // 4, w // 4, 4, 4, 4).transpose(0, 2, 1, 3, 4).reshape(h, 4 * w).astype(np.uint8)
+    img = np.ascontiguousarray(img)
+    for codec in (0, 1):
+        np.testing.assert_array_equal(_encode(emu, codec, img, w, h), oracle.encode(codec, img, w, h))
+
+
 def _decode(emu, codec, blocks, w, h):
     img = np.zeros((h, 4 * w), np.uint8)
     bad = emu.host_emu_decode(codec, np.ascontiguousarray(blocks).ctypes.data, w, h, img.ctypes.data, 4 * w)
