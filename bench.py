@@ -12,8 +12,11 @@ previous launch did not touch (inputs larger than the 129 MB L2).
                 (goofy_gpu_compress_host, the engine under goofy::compress*)
                 from pinned host memory, copies in and out inside the region.
 * roofline   -- dominant kernel: 4.5 algorithmic B/px (4 read + 0.5 written)
-                x pixels per launch / its mean CUDA-event duration, against
-                the measured HBM copy bandwidth.
+                x pixels per launch / its mean launch duration (K launches
+                back to back between two CUDA events, right after the timed
+                steps), against the measured HBM copy bandwidth.  No event
+                is recorded between two launches of a timed loop: one there
+                delays the next launch's start by a few microseconds.
 * cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
 
 ``--impl reference`` times the reference's CPU implementation of the path on
@@ -301,22 +304,22 @@ def run_two_streams(args, g, torch, src, dst, codecs, stream):
 
 def run_mips(g, torch, workloads, img, d_src, stream):
     """Device mip chain of the 8192x8192 image (levels 4096x4096 .. 4x4; up to
-    6 levels per launch): median time, HBM rate for the algorithmic bytes (the
+    6 levels per launch): mean time of 10 chains back to back, HBM rate for the algorithmic bytes (the
     image read once, every level written once) and equality with the host
     chain."""
     nbytes = g.lib().goofy_gpu_mip_arena_bytes(W, H)
     arena = torch.empty(nbytes + 256, dtype=torch.uint8, device=d_src.device)
     base = arena.data_ptr() + (-arena.data_ptr()) % 256
     sh = stream.cuda_stream
-    ts = []
-    for _ in range(10):
-        e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e_a.record(stream)
+    for _ in range(3):
         levels = g.generate_mips(d_src, W, H, 4 * W, base, nbytes, sh)
-        e_b.record(stream)
-        e_b.synchronize()
-        ts.append(e_a.elapsed_time(e_b))
-    ms = statistics.median(ts[3:])
+    e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_a.record(stream)
+    for _ in range(10):  # 10 chains back to back between two events
+        levels = g.generate_mips(d_src, W, H, 4 * W, base, nbytes, sh)
+    e_b.record(stream)
+    e_b.synchronize()
+    ms = e_a.elapsed_time(e_b) / 10
     moved = 4 * W * H + sum(4 * lw * lh for (_, lw, lh, _) in levels[1:])  # read the image once, write every level
     host = arena.cpu().numpy()
     off0 = base - arena.data_ptr()
@@ -626,15 +629,11 @@ def run_gpu(args):
     sh = stream.cuda_stream
     codecs = (g.CODEC_BC1, g.CODEC_ETC1S)
 
-    def step(events=None):
+    def step():
         for c in codecs:
-            if events is not None:
-                events[c][0].record(stream)
             rc = g.compress_device(c, dst[c].data_ptr(), src[c].data_ptr(), W, H, 4 * W, sh)
             if rc != g.OK:
                 raise RuntimeError("encode failed: %s %s" % (g.status_string(rc), g.last_error()))
-            if events is not None:
-                events[c][1].record(stream)
 
     def barrier():
         if world > 1:
@@ -672,23 +671,29 @@ def run_gpu(args):
             for _ in range(20):
                 step()
             torch.cuda.synchronize()
-        # timed region: K steps, CUDA events on the launching stream
-        per_launch = {c: [] for c in codecs}
-        ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for c in codecs]
-              for _ in range(args.steps)]
+        # timed region: K steps, CUDA events on the launching stream at its two ends only (an event
+        # recorded between two launches delays the second one's start by a few microseconds)
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         torch.cuda.synchronize()
         start.record(stream)
         for k in range(args.steps):
-            step(ev[k])
+            step()
         end.record(stream)
         torch.cuda.synchronize()
         barrier()
-    total_ms = start.elapsed_time(end)
-    for k in range(args.steps):
+        # each kernel's launch duration: K launches of it back to back between two events, the
+        # inputs alternating between the two 256 MiB copies (larger than L2 either way)
+        per_launch = {}
         for c in codecs:
-            per_launch[c].append(ev[k][c][0].elapsed_time(ev[k][c][1]))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for k in range(args.steps):
+                g.compress_device(c, dst[c].data_ptr(), src[(c + k) % 2].data_ptr(), W, H, 4 * W, sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            per_launch[c] = e0.elapsed_time(e1) / args.steps
+    total_ms = start.elapsed_time(end)
     total_ms = max_over_ranks(total_ms, world)
 
     px_per_step = 2 * W * H
@@ -746,13 +751,15 @@ def run_gpu(args):
     peak, peak_kind = read_peaks()
     per_codec = {}
     for c in codecs:
-        ms = statistics.mean(per_launch[c])
+        ms = per_launch[c]
         per_codec[names[c]] = {"mean_launch_us": round(1e3 * ms, 2),
-                               "median_launch_us": round(1e3 * statistics.median(per_launch[c]), 2),
                                "mpix_s": round(W * H / (ms / 1e3) / 1e6, 1),
                                "hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
-    dom = max(codecs, key=lambda c: statistics.mean(per_launch[c]))
-    dom_ms = statistics.mean(per_launch[dom])
+    per_codec["timing"] = ("mean of %d launches of the kernel back to back between two CUDA events, right after "
+                           "the timed steps; the step (%.2f us) also holds the switch from one kernel to the other"
+                           % (args.steps, 1e3 * total_ms / args.steps))
+    dom = max(codecs, key=lambda c: per_launch[c])
+    dom_ms = per_launch[dom]
     achieved = ALG_BYTES_PER_PX * W * H / (dom_ms / 1e3) / 1e9
     kernel = "encode_image_tma" if g.get_tile(dom)[2] == 2 else "encode_image_kernel"
     traffic = read_traffic("%s_%s_8192" % (kernel, names[dom]))
@@ -769,16 +776,16 @@ def run_gpu(args):
     for c in codecs:
         rc, psnr, sums = g.psnr_rgb(c, dst[c], src[c], W, H, 4 * W)
         assert rc == g.OK, g.last_error()
-        ts = []
-        for r in range(8):
-            d_sums.zero_()
-            e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e_a.record(stream)
+        # 10 launches back to back between two events (the sums only accumulate), after 2 untimed
+        for r in range(2):
             g.block_error_device(c, dst[c], src[(c + 1) % 2], W, H, 4 * W, d_sums, sh)
-            e_b.record(stream)
-            e_b.synchronize()
-            ts.append(e_a.elapsed_time(e_b))
-        ms = statistics.median(ts[2:])
+        e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_a.record(stream)
+        for r in range(10):
+            g.block_error_device(c, dst[c], src[(c + r) % 2], W, H, 4 * W, d_sums, sh)
+        e_b.record(stream)
+        e_b.synchronize()
+        ms = e_a.elapsed_time(e_b) / 10
         quality[names[c]] = {"psnr_rgb_db": round(psnr, 5), "unsupported_blocks": int(sums[4]),
                              "decode_error_kernel_us": round(ms * 1e3, 2),
                              "decode_error_hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}

@@ -298,7 +298,7 @@ def pipeline_timeouts(reset=False):
 
 def autotune(codec, dst, src, width, height, stride, reps=9):
     """Time every tile shape on a device image, install the fastest; returns
-    ((threads_per_cta, blocks_per_thread, persistent), median microseconds)."""
+    ((threads_per_cta, blocks_per_thread, persistent), mean microseconds a launch)."""
     t = Tile()
     us = ctypes.c_float()
     rc = lib().goofy_gpu_autotune(codec, _addr(dst), _addr(src), width, height, stride, reps, ctypes.byref(t),

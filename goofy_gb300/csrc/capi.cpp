@@ -430,7 +430,7 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
     int result = GOOFY_OK;
     Tile best_tile{0, 0, 0};
     float best_time = 0.f;
-    std::vector<float> times(reps);
+    std::vector<float> times(3);
     for (int i = 0; i < 2 && result == GOOFY_OK; ++i)
         if (cudaEventCreate(&ev[i]) != cudaSuccess) result = cuda_fail(cudaGetLastError(), "cudaEventCreate");
     std::vector<Tile> candidates;
@@ -445,21 +445,25 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
             return goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
                                            width, height, t, access, st);
         };
+        // three rounds of `reps` launches back to back between two events (an
+        // event between two launches would delay the second one's start); the
+        // median round's mean launch time
         cudaError_t e = cudaSuccess;
         for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = launch();
-        for (uint32_t r = 0; r < reps && e == cudaSuccess; ++r) {
+        for (uint32_t r = 0; r < 3 && e == cudaSuccess; ++r) {
             e = cudaEventRecord(ev[0], st);
-            if (e == cudaSuccess) e = launch();
+            for (uint32_t k = 0; k < reps && e == cudaSuccess; ++k) e = launch();
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
             if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
             if (e == cudaSuccess) e = cudaEventElapsedTime(&times[r], ev[0], ev[1]);
+            times[r] /= (float)reps;
         }
         if (e != cudaSuccess) {
             result = cuda_fail(e, "autotune launch");
             break;
         }
         std::sort(times.begin(), times.end());
-        const float med = times[reps / 2];
+        const float med = times[1];
         if (best_tile.threads == 0 || med < best_time) {
             best_time = med;
             best_tile = t;

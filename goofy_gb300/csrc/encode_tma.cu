@@ -34,9 +34,9 @@ struct TmaLayout {
     uint32_t tile_blocks, row_bytes, stage_bytes, stages;
 };
 
-__host__ __device__ inline TmaLayout tma_layout(uint32_t compute_threads, uint32_t bpt)
+__host__ __device__ constexpr TmaLayout tma_layout(uint32_t compute_threads, uint32_t bpt)
 {
-    TmaLayout l;
+    TmaLayout l{};
     l.tile_blocks = compute_threads * bpt;
     l.row_bytes = 16u * l.tile_blocks;
     l.stage_bytes = 4u * l.row_bytes;
@@ -47,17 +47,29 @@ __host__ __device__ inline TmaLayout tma_layout(uint32_t compute_threads, uint32
     return l;
 }
 
-inline size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * (l.stage_bytes + 16u) + 128u; }
+constexpr size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * (l.stage_bytes + 16u) + 128u; }
 
-template <int CODEC, int BPT>
-__global__ void __launch_bounds__(544) encode_image_tma(const uint8_t* __restrict__ src, size_t stride,
-                                                        uint8_t* __restrict__ dst, uint32_t bw, uint32_t tiles_per_row,
-                                                        uint32_t total_tiles, uint32_t tile_magic)
+// CTAs per SM each instantiation is compiled for (register caps that keep
+// that many resident; every ring fits that many times in shared memory).  With
+// two blocks a thread the ETC1s codec wants about 80 registers, so the
+// 512-thread CTA runs alone on its SM; the 256-thread one is capped at 72 to
+// fit 3.  The 128-thread CTA stays at 4: 5 would put 7 warps on one scheduler,
+// whose quarter of the register file then caps them at 72 with spills.
+__host__ __device__ constexpr int tma_min_ctas(int bpt, int compute_threads)
+{
+    return bpt == 1 ? (compute_threads == 512 ? 2 : compute_threads == 256 ? 4 : 7)
+                    : (compute_threads == 512 ? 1 : compute_threads == 256 ? 3 : 4);
+}
+
+template <int CODEC, int BPT, int COMPUTE>
+__global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
+    encode_image_tma(const uint8_t* __restrict__ src, size_t stride, uint8_t* __restrict__ dst, uint32_t bw,
+                     uint32_t tiles_per_row, uint32_t total_tiles, uint32_t tile_magic)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t abort_flag;
-    const uint32_t compute_warps = (blockDim.x >> 5) - 1u;
-    const TmaLayout L = tma_layout(compute_warps * 32u, BPT);
+    constexpr uint32_t compute_warps = COMPUTE / 32;
+    constexpr TmaLayout L = tma_layout(COMPUTE, BPT);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.stages * L.stage_bytes);
     uint64_t* empty = full + L.stages;
     uint8_t* ctrl_lut = reinterpret_cast<uint8_t*>(empty + L.stages);
@@ -145,47 +157,54 @@ __global__ void __launch_bounds__(544) encode_image_tma(const uint8_t* __restric
 
 namespace {
 
-template <int CODEC, int BPT>
-cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh, uint32_t threads,
+template <int CODEC, int BPT, int COMPUTE>
+cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
                          cudaStream_t stream)
 {
-    const TmaLayout L = tma_layout(threads, BPT);
+    constexpr TmaLayout L = tma_layout(COMPUTE, BPT);
     const size_t smem = tma_smem_bytes(L);
-    const uint32_t block = threads + 32u;
-    // per device: dynamic shared memory opt-in and resident CTAs per SM, by block size
-    static std::atomic<int> resident[64][3];
+    constexpr uint32_t block = COMPUTE + 32u;
+    // per device: dynamic shared memory opt-in and resident CTAs per SM
+    static std::atomic<int> resident[64];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    const int slot = threads == 128 ? 0 : threads == 256 ? 1 : 2;
-    int ctas = resident[dev][slot].load(std::memory_order_relaxed);
+    int ctas = resident[dev].load(std::memory_order_relaxed);
     if (ctas == 0) {
-        // the opt-in covers the largest ring of any block size of this instantiation
-        size_t most = 0;
-        for (uint32_t t : {128u, 256u, 512u}) {
-            const size_t b = tma_smem_bytes(tma_layout(t, BPT));
-            most = b > most ? b : most;
-        }
-        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT, COMPUTE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
+        e = cudaFuncSetAttribute(encode_image_tma<CODEC, BPT, COMPUTE>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_tma<CODEC, BPT>, (int)block, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_image_tma<CODEC, BPT, COMPUTE>, (int)block,
+                                                          smem);
         if (e != cudaSuccess) return e;
         ctas = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-        resident[dev][slot].store(ctas, std::memory_order_relaxed);
+        resident[dev].store(ctas, std::memory_order_relaxed);
     }
     const uint32_t tiles_per_row = (bw + L.tile_blocks - 1) / L.tile_blocks;
     const uint64_t total = (uint64_t)tiles_per_row * bh;
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;
     const uint32_t grid = (uint32_t)(total < (uint64_t)ctas ? total : (uint64_t)ctas);
-    encode_image_tma<CODEC, BPT><<<grid, block, smem, stream>>>(src, stride, dst, bw, tiles_per_row, (uint32_t)total,
-                                                               0xffffffffu / tiles_per_row);
+    encode_image_tma<CODEC, BPT, COMPUTE><<<grid, block, smem, stream>>>(src, stride, dst, bw, tiles_per_row,
+                                                                         (uint32_t)total, 0xffffffffu / tiles_per_row);
     return cudaGetLastError();
+}
+
+template <int CODEC, int BPT>
+cudaError_t launch_tma_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+                           uint32_t threads, cudaStream_t stream)
+{
+    switch (threads) {
+    case 128: return launch_tma_t<CODEC, BPT, 128>(src, stride, dst, bw, bh, stream);
+    case 256: return launch_tma_t<CODEC, BPT, 256>(src, stride, dst, bw, bh, stream);
+    case 512: return launch_tma_t<CODEC, BPT, 512>(src, stride, dst, bw, bh, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace
@@ -197,11 +216,11 @@ cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8
     if (bw == 0 || bh == 0) return cudaSuccess;
     if (reinterpret_cast<uintptr_t>(src) % 16 || stride % 16) return cudaErrorInvalidValue;
     if (codec == kBC1) {
-        if (tile.bpt == 1) return launch_tma_t<kBC1, 1>(src, stride, dst, bw, bh, tile.threads, stream);
-        if (tile.bpt == 2) return launch_tma_t<kBC1, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 1) return launch_tma_bpt<kBC1, 1>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_bpt<kBC1, 2>(src, stride, dst, bw, bh, tile.threads, stream);
     } else {
-        if (tile.bpt == 1) return launch_tma_t<kETC1S, 1>(src, stride, dst, bw, bh, tile.threads, stream);
-        if (tile.bpt == 2) return launch_tma_t<kETC1S, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 1) return launch_tma_bpt<kETC1S, 1>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_bpt<kETC1S, 2>(src, stride, dst, bw, bh, tile.threads, stream);
     }
     return cudaErrorInvalidValue;
 }

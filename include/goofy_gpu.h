@@ -119,9 +119,10 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
 
 /* Autotuner: times every tile shape on the caller's device image (`src`,
  * `dst` as for goofy_gpu_compress_device, on the current device) with CUDA
- * events -- `reps` timed launches per shape after two warm-up launches, median
- * kept -- installs the fastest as the codec's tile and returns it with its
- * median launch time in microseconds.  Synchronous.  No reference counterpart. */
+ * events -- after two warm-up launches, three rounds of `reps` launches back to
+ * back between two events, the median round's mean kept -- installs the
+ * fastest as the codec's tile and returns it with that mean launch time in
+ * microseconds.  Synchronous.  No reference counterpart. */
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
 
