@@ -55,7 +55,7 @@ using goofy_gpu::Tile;
 
 #define CUDA_TRY GOOFY_CUDA_TRY
 
-Tile g_tile[2] = {{128, 2, 0}, {128, 2, 2}};  // BC1: register-loading grid, ETC1s: bulk-copy pipeline; 2 blocks a thread
+Tile g_tile[2] = {{128, 2, 0}, {512, 2, 2}};  // BC1: register-loading grid, ETC1s: bulk-copy pipeline; 2 blocks a thread
 std::mutex g_tile_mu;
 
 Tile tile_for(int codec)

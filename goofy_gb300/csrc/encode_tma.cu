@@ -7,11 +7,11 @@
 // source) into the next free stage of a shared-memory ring with
 // cp.async.bulk, counted on that stage's "full" mbarrier; compute warps wait
 // for it, pull their blocks into registers with conflict-free 128-bit shared
-// loads (lane l of a warp reads 16 contiguous bytes, the warp 512), release
-// the stage on its "empty" mbarrier and run the same block codec as every
-// other kernel, storing 8 bytes per block with streaming stores.  Loads never
-// sit in the compute warps' registers, so the integer math of one tile
-// overlaps the HBM reads of the next stages.
+// loads (lane l of a warp reads 16 contiguous bytes, the warp 512), run the
+// same block codec as every other kernel, store 8 bytes per block with
+// streaming stores and release the stage on its "empty" mbarrier.  Global
+// loads never sit in the compute warps' registers, so the integer math of one
+// tile overlaps the HBM reads of the next stages.
 //
 // Needs 16-byte aligned source rows (base and stride); other images take the
 // register-loading kernels.  Every wait is bounded (async_copy.cuh): a stuck
@@ -30,6 +30,18 @@ namespace goofy_gpu {
 
 __device__ unsigned int g_pipeline_timeouts;
 
+// CTAs per SM each instantiation is compiled for (register caps that keep
+// that many resident; every ring fits that many times in shared memory).  With
+// two blocks a thread the ETC1s codec wants about 80 registers, so the
+// 512-thread CTA runs alone on its SM; the 256-thread one is capped at 72 to
+// fit 3.  The 128-thread CTA stays at 4: 5 would put 7 warps on one scheduler,
+// whose quarter of the register file then caps them at 72 with spills.
+__host__ __device__ constexpr int tma_min_ctas(uint32_t bpt, uint32_t compute_threads)
+{
+    return bpt == 1 ? (compute_threads == 512 ? 2 : compute_threads == 256 ? 4 : 7)
+                    : (compute_threads == 512 ? 1 : compute_threads == 256 ? 3 : 4);
+}
+
 struct TmaLayout {
     uint32_t tile_blocks, row_bytes, stage_bytes, stages;
 };
@@ -41,25 +53,16 @@ __host__ __device__ constexpr TmaLayout tma_layout(uint32_t compute_threads, uin
     l.row_bytes = 16u * l.tile_blocks;
     l.stage_bytes = 4u * l.row_bytes;
     // ring budget scaled with the CTA (112 KB at 512 compute threads), so the
-    // CTAs the registers allow per SM also fit in shared memory
+    // CTAs the registers allow per SM also fit in shared memory; at least 3
+    // stages for a CTA alone on its SM (a stage is released only once it has
+    // been encoded, so 2 would leave that SM a single stage of lookahead)
     const uint32_t s = (114688u / 512u * compute_threads) / l.stage_bytes;
-    l.stages = s < 2u ? 2u : s > 6u ? 6u : s;
+    const uint32_t lo = tma_min_ctas(bpt, compute_threads) == 1 ? 3u : 2u;
+    l.stages = s < lo ? lo : s > 6u ? 6u : s;
     return l;
 }
 
 constexpr size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * (l.stage_bytes + 16u) + 128u; }
-
-// CTAs per SM each instantiation is compiled for (register caps that keep
-// that many resident; every ring fits that many times in shared memory).  With
-// two blocks a thread the ETC1s codec wants about 80 registers, so the
-// 512-thread CTA runs alone on its SM; the 256-thread one is capped at 72 to
-// fit 3.  The 128-thread CTA stays at 4: 5 would put 7 warps on one scheduler,
-// whose quarter of the register file then caps them at 72 with spills.
-__host__ __device__ constexpr int tma_min_ctas(int bpt, int compute_threads)
-{
-    return bpt == 1 ? (compute_threads == 512 ? 2 : compute_threads == 256 ? 4 : 7)
-                    : (compute_threads == 512 ? 1 : compute_threads == 256 ? 3 : 4);
-}
 
 template <int CODEC, int BPT, int COMPUTE>
 __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
@@ -140,14 +143,22 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
                 }
             }
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[slot]);
         uint8_t* out = dst + ((size_t)by * bw + bx0) * 8u;
 #pragma unroll
         for (int j = 0; j < BPT; ++j) {
             const uint32_t b = (warp * BPT + j) * 32u + lane;
             if (b < nb) st_stream8(out + 8u * (size_t)b, encode_block<CODEC>(w[j], ctrl_lut));
         }
+        // Release the stage only now.  An arrival right after the shared loads
+        // can overtake them: the loads wait in the load/store queue (behind
+        // other kernels' global loads when SMs are shared) while the arrival
+        // completes at once, and the producer's next copy into the stage then
+        // lands before they read it (seen with a concurrent register-loading
+        // kernel: rows of the stage's next tile inside this tile's blocks).
+        // The stores cannot issue before the blocks they write are encoded
+        // from every loaded word, and the arrival (a release) stays after them.
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
         if (++slot == L.stages) {
             slot = 0;
             phase ^= 1u;

@@ -162,6 +162,45 @@ def test_full_size_stress_4096(cuda, name, codec):
         np.testing.assert_array_equal(part.reshape(h // 4, q // 4, 8), full[:, k * q // 4:(k + 1) * q // 4])
 
 
+def test_concurrent_kernels_bit_exact(cuda):
+    """The two codecs on two streams at once, one through the bulk-copy
+    pipeline and the other through a register-loading kernel sharing its SMs
+    (whose global loads crowd the load/store queues), each output equal to the
+    oracle's.  A compute warp that released its ring stage before its shared
+    loads had read it once let the stage's next tile overwrite rows of the
+    current one in exactly this setting."""
+    w = h = 8192
+    img = workloads.scene(w, h, 1, period_scale=32, rects=2048, threads=0)
+    want = [cuda.from_numpy(oracle.encode(c, img, w, h, threads=0)).cuda() for c in (0, 1)]
+    src = [cuda.from_numpy(img.reshape(-1)).cuda() for _ in range(2)]
+    outs = [cuda.empty(g.out_size(w, h), dtype=cuda.uint8, device="cuda") for _ in range(2)]
+    streams = [cuda.cuda.current_stream(), cuda.cuda.Stream()]
+    before = [g.get_tile(c) for c in (0, 1)]
+    g.pipeline_timeouts(reset=True)
+    try:
+        for pipe in (1, 0):  # the codec on the bulk-copy kernel
+            for pipe_tile in ((128, 2, 2), (128, 1, 2), (512, 1, 2), (512, 2, 2), (256, 1, 2)):
+                for grid_tile in ((128, 2, 0), (128, 1, 0)):
+                    assert g.set_tile(pipe, *pipe_tile) == g.OK
+                    assert g.set_tile(1 - pipe, *grid_tile) == g.OK
+                    for _ in range(4):
+                        for o in outs:
+                            o.zero_()
+                        ev = cuda.cuda.Event()
+                        ev.record(streams[0])
+                        streams[1].wait_event(ev)
+                        for c in (pipe, 1 - pipe):  # the pipelined kernel first, so it is resident when the other starts
+                            assert g.compress_device(c, outs[c].data_ptr(), src[c].data_ptr(), w, h, 4 * w,
+                                                     streams[c].cuda_stream) == g.OK
+                        cuda.cuda.synchronize()
+                        for c in (0, 1):
+                            assert cuda.equal(outs[c], want[c]), (pipe, pipe_tile, grid_tile, c)
+    finally:
+        for c in (0, 1):
+            g.set_tile(c, *before[c])
+    assert g.pipeline_timeouts() == 0
+
+
 def test_pipeline_reports_no_timeouts(cuda):
     """The bulk-copy pipeline's bounded waits never expire in a healthy run."""
     g.pipeline_timeouts(reset=True)
