@@ -68,15 +68,26 @@ __device__ __forceinline__ void accumulate_row(const uint32_t (&a)[4], const uin
 
 // The harness's luminosity difference (0.21 R + 0.72 G + 0.07 B of a pixel
 // read as a little-endian u32, R = byte 2) in hundredths, which is exact in
-// integers: 21 * d(byte 2) + 72 * d(byte 1) + 7 * d(byte 0); squared and
-// summed over a row of 4 pixels (at most 4 * 25500^2 < 2^32).
+// integers: 21 * d(byte 2) + 72 * d(byte 1) + 7 * d(byte 0).  Two byte dot
+// products: the second multiplies b's unsigned bytes by the negated weights
+// (signed bytes) and adds the first, so no subtraction is needed.
+__device__ __forceinline__ int luma_diff(uint32_t a, uint32_t b)
+{
+    constexpr uint32_t kWeights = 0x00154807u;     // bytes 0..3: 7, 72, 21, 0
+    constexpr uint32_t kNegWeights = 0x00ebb8f9u;  // bytes 0..3: -7, -72, -21, 0
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(b), "r"(kNegWeights), "r"((int)__dp4a(a, kWeights, 0u)));
+    return d;
+}
+
+// Squared luminosity differences summed over a row of 4 pixels (at most
+// 4 * 25500^2 < 2^32).
 __device__ __forceinline__ uint32_t luma_row(const uint32_t (&a)[4], const uint32_t (&b)[4])
 {
-    constexpr uint32_t kWeights = 0x00154807u;  // bytes 0..3: 7, 72, 21, 0
     uint32_t acc = 0;
 #pragma unroll
     for (int x = 0; x < 4; ++x) {
-        const int d = (int)__dp4a(a[x], kWeights, 0u) - (int)__dp4a(b[x], kWeights, 0u);
+        const int d = luma_diff(a[x], b[x]);
         acc += (uint32_t)(d * d);
     }
     return acc;
