@@ -18,6 +18,7 @@
 #include "block_decode.cuh"
 #include "decode.h"
 #include "device_io.cuh"
+#include "pdl.cuh"
 
 namespace goofy_gpu {
 
@@ -33,9 +34,11 @@ __global__ void __launch_bounds__(256) decode_image_kernel(const uint8_t* __rest
                                                            uint32_t nblk, uint8_t* __restrict__ rgba, size_t stride,
                                                            unsigned long long* __restrict__ unsupported)
 {
+    pdl_launch_dependents();
     __shared__ uint32_t pal[8 * 256];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool ok = true;
+    pdl_wait();
     if (i < nblk) {
         const uint32_t by = i / bw, bx = i - by * bw;
         uint32_t px[16];
@@ -102,9 +105,11 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
                                                           size_t stride, bool vec16,
                                                           unsigned long long* __restrict__ sums)
 {
+    pdl_launch_dependents();
     __shared__ uint32_t pal[8 * 256];
     unsigned long long s[6] = {0, 0, 0, 0, 0, 0};
     const uint32_t bw_magic = 0xffffffffu / bw;
+    pdl_wait();
     // software pipeline: the next block's source rows and code are loaded
     // before this block is decoded and compared
     const uint32_t step = gridDim.x * blockDim.x;
@@ -232,9 +237,11 @@ cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint
     const uint32_t bw = width / 4, nblk = bw * (height / 4);
     if (nblk == 0) return cudaSuccess;
     const uint32_t grid = (nblk + 255) / 256;
-    if (codec == kBC1) decode_image_kernel<kBC1><<<grid, 256, 0, stream>>>(blocks, bw, nblk, rgba, stride, unsupported);
-    else decode_image_kernel<kETC1S><<<grid, 256, 0, stream>>>(blocks, bw, nblk, rgba, stride, unsupported);
-    return cudaGetLastError();
+    if (codec == kBC1)
+        return launch_pdl(decode_image_kernel<kBC1>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, rgba, stride,
+                          unsupported);
+    return launch_pdl(decode_image_kernel<kETC1S>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, rgba, stride,
+                      unsupported);
 }
 
 cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* src, uint32_t width, uint32_t height,
@@ -247,10 +254,10 @@ cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t grid = min((nblk + 255) / 256, (uint32_t)(sms > 0 ? sms : 1) * 8u);
     if (codec == kBC1)
-        block_error_kernel<kBC1><<<grid, 256, 0, stream>>>(blocks, bw, nblk, src, stride, vec16, sums);
-    else
-        block_error_kernel<kETC1S><<<grid, 256, 0, stream>>>(blocks, bw, nblk, src, stride, vec16, sums);
-    return cudaGetLastError();
+        return launch_pdl(block_error_kernel<kBC1>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, src, stride,
+                          vec16, sums);
+    return launch_pdl(block_error_kernel<kETC1S>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, src, stride,
+                      vec16, sums);
 }
 
 }  // namespace goofy_gpu

@@ -19,6 +19,7 @@
 #include "block_codec.cuh"
 #include "device_io.cuh"
 #include "kernels.h"
+#include "pdl.cuh"
 
 namespace goofy_gpu {
 
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __rest
                                                            uint32_t total_segs, uint32_t segs_per_row,
                                                            uint32_t seg_magic)
 {
+    pdl_launch_dependents();
     __shared__ uint8_t ctrl_lut[128];
     if constexpr (CODEC == kETC1S) {
         fill_ctrl_lut(ctrl_lut);
@@ -79,6 +81,7 @@ __global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __rest
     }
     const uint32_t seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (seg >= total_segs) return;
+    pdl_wait();
     uint32_t w[BPT][16];
     const Segment sg = load_segment<BPT, ACCESS>(src, stride, bw, seg, segs_per_row, seg_magic, threadIdx.x & 31u, w);
     encode_segment<CODEC, BPT>(dst, bw, sg, w, ctrl_lut);
@@ -90,11 +93,13 @@ __global__ void __launch_bounds__(512) encode_image_persistent(const uint8_t* __
                                                                uint32_t total_segs, uint32_t segs_per_row,
                                                                uint32_t seg_magic)
 {
+    pdl_launch_dependents();
     __shared__ uint8_t ctrl_lut[128];
     if constexpr (CODEC == kETC1S) {
         fill_ctrl_lut(ctrl_lut);
         __syncthreads();
     }
+    pdl_wait();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp_stride = gridDim.x * (blockDim.x >> 5);
     uint32_t seg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -165,14 +170,12 @@ static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uin
         if (persistent) {
             const uint64_t resident = (uint64_t)resident_ctas<CODEC, BPT, ACCESS>(threads);
             if (ctas > resident) ctas = resident;
-            encode_image_persistent<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(
-                src, stride, dst, bw, (uint32_t)total, segs, magic);
-            return cudaGetLastError();
+            return launch_pdl(encode_image_persistent<CODEC, BPT, ACCESS>, dim3((unsigned)ctas), dim3(threads), 0,
+                              stream, src, stride, dst, bw, (uint32_t)total, segs, magic);
         }
     }
-    encode_image_kernel<CODEC, BPT, ACCESS><<<(unsigned)ctas, threads, 0, stream>>>(src, stride, dst, bw,
-                                                                                   (uint32_t)total, segs, magic);
-    return cudaGetLastError();
+    return launch_pdl(encode_image_kernel<CODEC, BPT, ACCESS>, dim3((unsigned)ctas), dim3(threads), 0, stream, src,
+                      stride, dst, bw, (uint32_t)total, segs, magic);
 }
 
 template <int CODEC, SrcAccess ACCESS>

@@ -25,6 +25,7 @@
 #include "block_codec.cuh"
 #include "device_io.cuh"
 #include "kernels.h"
+#include "pdl.cuh"
 
 namespace goofy_gpu {
 
@@ -69,6 +70,7 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     encode_image_tma(const uint8_t* __restrict__ src, size_t stride, uint8_t* __restrict__ dst, uint32_t bw,
                      uint32_t tiles_per_row, uint32_t total_tiles, uint32_t tile_magic)
 {
+    pdl_launch_dependents();
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t abort_flag;
     constexpr uint32_t compute_warps = COMPUTE / 32;
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     }
     if constexpr (CODEC == kETC1S) fill_ctrl_lut(ctrl_lut);
     __syncthreads();
+    pdl_wait();  // no global memory before the previous kernel in the stream is done
 
     if (warp == compute_warps) {  // producer
         if (lane != 0) return;
@@ -201,9 +204,8 @@ cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32
     const uint64_t total = (uint64_t)tiles_per_row * bh;
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;
     const uint32_t grid = (uint32_t)(total < (uint64_t)ctas ? total : (uint64_t)ctas);
-    encode_image_tma<CODEC, BPT, COMPUTE><<<grid, block, smem, stream>>>(src, stride, dst, bw, tiles_per_row,
-                                                                         (uint32_t)total, 0xffffffffu / tiles_per_row);
-    return cudaGetLastError();
+    return launch_pdl(encode_image_tma<CODEC, BPT, COMPUTE>, dim3(grid), dim3(block), smem, stream, src, stride, dst,
+                      bw, tiles_per_row, (uint32_t)total, 0xffffffffu / tiles_per_row);
 }
 
 template <int CODEC, int BPT>

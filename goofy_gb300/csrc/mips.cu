@@ -16,6 +16,7 @@
 
 #include "../../include/goofy_gpu.h"
 #include "host_util.h"
+#include "pdl.cuh"
 
 namespace {
 
@@ -35,8 +36,10 @@ __global__ void __launch_bounds__(256) mip_level_kernel(const uint8_t* __restric
                                                         uint8_t* __restrict__ dst, size_t dst_stride, uint32_t dw,
                                                         uint32_t dh, uint32_t fx, uint32_t fy)
 {
+    goofy_gpu::pdl_launch_dependents();
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= dw || y >= dh) return;
+    goofy_gpu::pdl_wait();
     const uint8_t* r0 = src + (size_t)(y * fy) * src_stride + 4u * (size_t)(x * fx);
     const uint8_t* r1 = r0 + src_stride * (fy - 1);
     uint32_t a, b, c, d;
@@ -125,12 +128,14 @@ template <int TILES>
 __global__ void __launch_bounds__(256) mip_fused_kernel(const uint8_t* __restrict__ src, size_t src_stride,
                                                         uint32_t tw_log2, uint32_t th_log2, uint32_t nlev, MipOut out)
 {
+    goofy_gpu::pdl_launch_dependents();
     __shared__ uint32_t buf[2][64];
     const uint32_t t = threadIdx.x, ty = blockIdx.y;
     const uint32_t w2_log2 = tw_log2 - 2, h2_log2 = th_log2 - 2, w2 = 1u << w2_log2;
     const bool act = t < (1u << (w2_log2 + h2_log2));
     const uint32_t x2 = t & (w2 - 1u), y2 = t >> w2_log2;
     uint4 r[TILES][4];
+    goofy_gpu::pdl_wait();  // the level above may come from the previous launch
 #pragma unroll
     for (int k = 0; k < TILES; ++k) {
         if (act) {
@@ -225,13 +230,14 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
                 mo.pitch[l] = levels[i + l].stride;
             }
             const uint32_t gx = up.width / tw, gy = up.height / th;
+            const uint8_t* up_data = static_cast<const uint8_t*>(up.data);
+            const size_t up_stride = up.stride;
             if (gx % 2 == 0)  // (two tiles per CTA measured faster than one or four)
-                mip_fused_kernel<2><<<dim3(gx / 2, gy), 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
-                                                                      log2u(tw), log2u(th), f, mo);
+                GOOFY_CUDA_TRY(goofy_gpu::launch_pdl(mip_fused_kernel<2>, dim3(gx / 2, gy), dim3(256), 0, st, up_data,
+                                                     up_stride, log2u(tw), log2u(th), f, mo));
             else
-                mip_fused_kernel<1><<<dim3(gx, gy), 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
-                                                                  log2u(tw), log2u(th), f, mo);
-            GOOFY_CUDA_TRY(cudaGetLastError());
+                GOOFY_CUDA_TRY(goofy_gpu::launch_pdl(mip_fused_kernel<1>, dim3(gx, gy), dim3(256), 0, st, up_data,
+                                                     up_stride, log2u(tw), log2u(th), f, mo));
             i += f;
             continue;
         }
@@ -239,15 +245,15 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
         const uint32_t fx = up.width > lv.width ? 2 : 1, fy = up.height > lv.height ? 2 : 1;
         const bool pair = fx == 2 && reinterpret_cast<uintptr_t>(up.data) % 8 == 0 && up.stride % 8 == 0;
         const dim3 grid((lv.width + 255) / 256, lv.height);
+        const uint8_t* up_data = static_cast<const uint8_t*>(up.data);
+        uint8_t* lv_data = static_cast<uint8_t*>(lv.data);
+        const size_t up_stride = up.stride, lv_stride = lv.stride;
         if (pair)
-            mip_level_kernel<true><<<grid, 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
-                                                         static_cast<uint8_t*>(lv.data), lv.stride, lv.width,
-                                                         lv.height, fx, fy);
+            GOOFY_CUDA_TRY(goofy_gpu::launch_pdl(mip_level_kernel<true>, grid, dim3(256), 0, st, up_data, up_stride,
+                                                 lv_data, lv_stride, lv.width, lv.height, fx, fy));
         else
-            mip_level_kernel<false><<<grid, 256, 0, st>>>(static_cast<const uint8_t*>(up.data), up.stride,
-                                                          static_cast<uint8_t*>(lv.data), lv.stride, lv.width,
-                                                          lv.height, fx, fy);
-        GOOFY_CUDA_TRY(cudaGetLastError());
+            GOOFY_CUDA_TRY(goofy_gpu::launch_pdl(mip_level_kernel<false>, grid, dim3(256), 0, st, up_data, up_stride,
+                                                 lv_data, lv_stride, lv.width, lv.height, fx, fy));
         ++i;
     }
     *nlevels = n;
