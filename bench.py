@@ -14,7 +14,8 @@ previous launch did not touch (inputs larger than the 129 MB L2).
 * roofline   -- dominant kernel: 4.5 algorithmic B/px (4 read + 0.5 written)
                 x pixels per launch / its mean launch duration (K launches
                 back to back between two CUDA events, right after the timed
-                steps), against the measured HBM copy bandwidth.  No event
+                steps, inputs and outputs alternating between two buffers
+                each), against the measured HBM copy bandwidth.  No event
                 is recorded between two launches of a timed loop: one there
                 delays the next launch's start by a few microseconds.
 * cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
@@ -625,6 +626,7 @@ def run_gpu(args):
     src[1] = src[0].clone()
     n_out = g.out_size(W, H)
     dst = [torch.empty(n_out, dtype=torch.uint8, device=dev) for _ in range(2)]
+    scratch = [torch.empty(n_out, dtype=torch.uint8, device=dev) for _ in range(2)]
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     codecs = (g.CODEC_BC1, g.CODEC_ETC1S)
@@ -683,13 +685,14 @@ def run_gpu(args):
         torch.cuda.synchronize()
         barrier()
         # each kernel's launch duration: K launches of it back to back between two events, the
-        # inputs alternating between the two 256 MiB copies (larger than L2 either way)
+        # inputs alternating between the two 256 MiB copies (larger than L2 either way) and the
+        # outputs between two scratch buffers (no launch rewrites the lines the previous one wrote)
         per_launch = {}
         for c in codecs:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for k in range(args.steps):
-                g.compress_device(c, dst[c].data_ptr(), src[(c + k) % 2].data_ptr(), W, H, 4 * W, sh)
+                g.compress_device(c, scratch[k % 2].data_ptr(), src[(c + k) % 2].data_ptr(), W, H, 4 * W, sh)
             e1.record(stream)
             torch.cuda.synchronize()
             per_launch[c] = e0.elapsed_time(e1) / args.steps
@@ -756,8 +759,9 @@ def run_gpu(args):
                                "mpix_s": round(W * H / (ms / 1e3) / 1e6, 1),
                                "hbm_gbs": round(ALG_BYTES_PER_PX * W * H / (ms / 1e3) / 1e9, 1)}
     per_codec["timing"] = ("mean of %d launches of the kernel back to back between two CUDA events, right after "
-                           "the timed steps; the step (%.2f us) also holds the switch from one kernel to the other"
-                           % (args.steps, 1e3 * total_ms / args.steps))
+                           "the timed steps, inputs and outputs alternating between two buffers each; the step "
+                           "(%.2f us) also holds the switch from one kernel to the other" % (args.steps,
+                                                                                           1e3 * total_ms / args.steps))
     dom = max(codecs, key=lambda c: per_launch[c])
     dom_ms = per_launch[dom]
     achieved = ALG_BYTES_PER_PX * W * H / (dom_ms / 1e3) / 1e9

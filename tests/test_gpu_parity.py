@@ -201,6 +201,47 @@ def test_concurrent_kernels_bit_exact(cuda):
     assert g.pipeline_timeouts() == 0
 
 
+def test_back_to_back_launches_keep_stream_order(cuda):
+    """Encoder launches back to back on one stream without synchronisation,
+    each one touching memory the previous one reads or writes.  The encoders
+    may be scheduled while the previous kernel drains (programmatic dependent
+    launch), but must not touch global memory before it is done: B overwrites
+    the source A reads, C encodes again into the blocks A wrote, D reads C's
+    blocks (decode + error sums)."""
+    w = h = 2048
+    img = workloads.scene(w, h, 5, threads=0)
+    other = workloads.stress(w, h, 6)
+    n = g.out_size(w, h)
+    st = cuda.cuda.current_stream().cuda_stream
+    before = [g.get_tile(c) for c in (0, 1)]
+    try:
+        for tiles in ((before[0], before[1]), ((128, 1, 0), (128, 2, 2)), ((512, 1, 2), (128, 2, 0))):
+            for c in (0, 1):
+                assert g.set_tile(c, *tiles[c]) == g.OK
+            for ca, cb in ((0, 1), (1, 0), (1, 1)):
+                work = cuda.from_numpy(img.reshape(-1)).cuda()
+                oth = cuda.from_numpy(other.reshape(-1)).cuda()
+                out = cuda.empty(n, dtype=cuda.uint8, device="cuda")
+                sums = cuda.zeros(6, dtype=cuda.int64, device="cuda")
+                cuda.cuda.synchronize()
+                assert g.compress_device(ca, out.data_ptr(), work.data_ptr(), w, h, 4 * w, st) == g.OK      # A
+                assert g.compress_device(cb, work.data_ptr(), oth.data_ptr(), w, h, 4 * w, st) == g.OK      # B
+                first = out.clone()
+                assert g.compress_device(cb, out.data_ptr(), oth.data_ptr(), w, h, 4 * w, st) == g.OK       # C
+                assert g.block_error_device(cb, out, oth, w, h, 4 * w, sums, st) == g.OK                    # D
+                cuda.cuda.synchronize()
+                np.testing.assert_array_equal(first.cpu().numpy(), oracle.encode(ca, img, w, h))
+                want_b = oracle.encode(cb, other, w, h)
+                np.testing.assert_array_equal(work[:n].cpu().numpy(), want_b)
+                np.testing.assert_array_equal(out.cpu().numpy(), want_b)
+                dec, _ = oracle.decode(cb, want_b, w, h)
+                np.testing.assert_array_equal(sums.cpu().numpy()[:4].astype(np.uint64),
+                                              oracle.sq_error(other, dec, w, h))
+    finally:
+        for c in (0, 1):
+            g.set_tile(c, *before[c])
+
+
 def test_pipeline_reports_no_timeouts(cuda):
     """The bulk-copy pipeline's bounded waits never expire in a healthy run."""
     g.pipeline_timeouts(reset=True)
