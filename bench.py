@@ -125,7 +125,7 @@ class ClockSampler:
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,clocks.max.mem")
 
     def __init__(self, index):
         self.index = index
@@ -152,7 +152,7 @@ class ClockSampler:
             self.lines = [l for l in out.splitlines() if l.strip()]
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
+        sm, mx, mem, mem_mx, power, reasons = [], [], [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for l in getattr(self, "lines", []):
             f = [x.strip() for x in l.split(",")]
@@ -166,10 +166,19 @@ class ClockSampler:
             for n, v in zip(names, f[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
+            try:  # memory clock and power: reported beside the SM clock, not used to accept a run
+                power.append(float(f[3]))
+                mem.append(float(f[9]))
+                mem_mx.append(float(f[10]))
+            except (ValueError, IndexError):
+                pass
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if mem:
+            out.update(mem_mhz=statistics.median(mem), mem_max_mhz=max(mem_mx), power_w=statistics.median(power))
+        return out
 
 
 def cpu_encode_all(lib_fn, img, threads, outs=None):

@@ -1,0 +1,53 @@
+"""bench.py's host-side bookkeeping on CPU: the clock record taken during the
+timed region, the committed per-launch DRAM traffic the roofline quotes, and
+the peak it is measured against."""
+import json
+import os
+
+import bench
+
+ROW = "0, {sm}, 2070, 900.0, 0x0, {hw}, Not Active, Not Active, {cap}, 3996, 3996"
+
+
+def _summary(lines):
+    c = bench.ClockSampler(0)
+    c.lines = lines
+    return c.summary()
+
+
+def test_clock_summary_median_reasons_and_memory_clock():
+    s = _summary([ROW.format(sm=2070, hw="Not Active", cap="Not Active"),
+                  ROW.format(sm=1980, hw="Not Active", cap="Active"),
+                  ROW.format(sm=2070, hw="Not Active", cap="Not Active")])
+    assert s["sm_mhz"] == 2070 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"]
+    assert s["mem_mhz"] == 3996 and s["mem_max_mhz"] == 3996 and s["power_w"] == 900.0
+    assert _summary([ROW.format(sm=1500, hw="Active", cap="Not Active")])["reasons"] == ["hw_slowdown"]
+
+
+def test_clock_summary_without_samples_or_memory_fields():
+    assert _summary([])["samples"] == 0
+    short = "0, 2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, Not Active"
+    s = _summary([short, "garbage", ""])
+    assert s["samples"] == 1 and "mem_mhz" not in s
+
+
+def test_roofline_traffic_comes_from_the_committed_profiles():
+    """Every kernel the roofline can name has its ncu read + write bytes in
+    profiles/, and they are close to the algorithmic 4.5 B/px of a launch
+    (less where L2 still holds part of the output at the end)."""
+    algorithmic = 4.5 * 8192 * 8192
+    for key in ("encode_image_kernel_bc1_8192", "encode_image_tma_etc1s_8192"):
+        t = bench.read_traffic(key)
+        assert t is not None, key
+        assert 0.9 * algorithmic < t <= 1.02 * algorithmic, (key, t)
+    assert bench.read_traffic("no_such_kernel") is None
+
+
+def test_peak_is_the_measured_copy_bandwidth():
+    peak, kind = bench.read_peaks()
+    path = os.path.join(bench.ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        assert kind == "measured" and peak == float(json.load(open(path))["hbm_gbs"])
+    else:
+        assert (peak, kind) == (6800.0, "fallback")
