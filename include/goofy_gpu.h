@@ -57,7 +57,12 @@ const char* goofy_gpu_last_error(void);
  * src: device RGBA8, `stride` bytes per row (4-byte aligned; 16-byte aligned
  * src and stride take the vector-load path).  dst: device, 8-byte aligned,
  * (width/4)*(height/4)*8 bytes.  width % 4 == 0 (not % 16: blocks are
- * independent), height % 4 == 0.  Enqueues one kernel on `stream`; no sync. */
+ * independent), height % 4 == 0.  Enqueues one kernel on `stream`; no sync.
+ * The kernel is launched with programmatic stream serialization: after one of
+ * this library's kernels its CTAs may be scheduled while that kernel drains,
+ * but they touch no global memory before it has completed, so stream order
+ * holds for every buffer (after any other kernel or copy it starts when that
+ * one completes).  The decoders and the mip generator launch the same way. */
 int goofy_gpu_compress_bc1_device(void* dst, const void* src, uint32_t width, uint32_t height,
                                   uint32_t stride, void* stream);
 
