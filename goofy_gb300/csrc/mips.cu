@@ -219,10 +219,12 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
         // levels from here on that halve both axes (an axis at 4 stays 4)
         uint32_t both = 0;
         for (uint32_t w = up.width, h = up.height; i + both < n && w > 4 && h > 4; w /= 2, h /= 2) ++both;
-        const uint32_t tw = up.width < 64 ? up.width : 64, th = up.height < 64 ? up.height : 64;
-        uint32_t f = log2u(tw < th ? tw : th);
+        uint32_t f = log2u(up.width < up.height ? up.width : up.height);
         f = f < both ? f : both;
         f = f < 6 ? f : 6;
+        // square tiles of 2^f pixels make exactly f levels (one pixel of the last);
+        // the tail of a chain thus gets many small tiles instead of a few large ones
+        const uint32_t tw = 1u << f, th = 1u << f;
         if (f >= 2 && reinterpret_cast<uintptr_t>(up.data) % 16 == 0 && up.stride % 16 == 0) {
             MipOut mo{};
             for (uint32_t l = 0; l < f; ++l) {
@@ -232,7 +234,7 @@ GOOFY_EXPORT int goofy_gpu_generate_mips(const void* src, uint32_t width, uint32
             const uint32_t gx = up.width / tw, gy = up.height / th;
             const uint8_t* up_data = static_cast<const uint8_t*>(up.data);
             const size_t up_stride = up.stride;
-            if (gx % 2 == 0)  // (two tiles per CTA measured faster than one or four)
+            if (gx % 2 == 0 && (uint64_t)gx * gy >= 2048)  // two tiles a CTA (faster than one or four) on large grids
                 GOOFY_CUDA_TRY(goofy_gpu::launch_pdl(mip_fused_kernel<2>, dim3(gx / 2, gy), dim3(256), 0, st, up_data,
                                                      up_stride, log2u(tw), log2u(th), f, mo));
             else
