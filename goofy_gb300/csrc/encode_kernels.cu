@@ -11,7 +11,9 @@
 // 8-byte block store of the warp writes 256 contiguous bytes.  Source rows are
 // read once (L1 no-allocate) and blocks are written with streaming stores:
 // the kernel moves 4 B/px in and 0.5 B/px out and is meant to sit on the HBM
-// roofline.
+// roofline.  Launched with programmatic dependent launch (pdl.cuh): CTAs may
+// start while the previous kernel in the stream drains and wait for it before
+// their first load.
 #include <cuda_runtime.h>
 
 #include <atomic>

@@ -13,6 +13,10 @@
 // loads never sit in the compute warps' registers, so the integer math of one
 // tile overlaps the HBM reads of the next stages.
 //
+// Launched with programmatic dependent launch (pdl.cuh): the prologue
+// (barriers, control-byte table) runs while the previous kernel in the stream
+// drains, and no copy is issued before that kernel has completed.
+//
 // Needs 16-byte aligned source rows (base and stride); other images take the
 // register-loading kernels.  Every wait is bounded (async_copy.cuh): a stuck
 // barrier ends the kernel with a counted time-out instead of a hang, and the
