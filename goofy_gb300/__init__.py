@@ -100,7 +100,7 @@ class Image(ctypes.Structure):
 
 class BatchTile(ctypes.Structure):
     _fields_ = [("threads_per_cta", ctypes.c_uint32), ("blocks_per_thread", ctypes.c_uint32),
-                ("unit_blocks", ctypes.c_uint32)]
+                ("unit_blocks", ctypes.c_uint32), ("pipeline", ctypes.c_uint32)]
 
 
 def _declare(lib):
@@ -339,12 +339,13 @@ class Batch:
         return lib().goofy_gpu_batch_set_graphs(self._h, 1 if enable else 0)
 
     def get_tile(self):
+        """(threads_per_cta, blocks_per_thread, unit_blocks, pipeline)"""
         t = BatchTile()
         assert lib().goofy_gpu_batch_get_tile(self._h, ctypes.byref(t)) == OK
-        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks)
+        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks, t.pipeline)
 
-    def set_tile(self, threads_per_cta, blocks_per_thread, unit_blocks):
-        t = BatchTile(threads_per_cta, blocks_per_thread, unit_blocks)
+    def set_tile(self, threads_per_cta, blocks_per_thread, unit_blocks, pipeline=0):
+        t = BatchTile(threads_per_cta, blocks_per_thread, unit_blocks, pipeline)
         return lib().goofy_gpu_batch_set_tile(self._h, ctypes.byref(t))
 
     def autotune(self, images, reps=5):
@@ -354,7 +355,7 @@ class Batch:
         rc = lib().goofy_gpu_batch_autotune(self._h, arr, len(arr), reps, ctypes.byref(t), ctypes.byref(us))
         if rc != OK:
             raise RuntimeError("batch autotune: %s %s" % (status_string(rc), last_error()))
-        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks), us.value
+        return (t.threads_per_cta, t.blocks_per_thread, t.unit_blocks, t.pipeline), us.value
 
     def close(self):
         if self._h:

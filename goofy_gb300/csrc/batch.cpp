@@ -6,12 +6,13 @@
 // owns two descriptor slots (pinned host staging + device table + work
 // counter).  Slots alternate between calls, so the descriptors of the next
 // batch are written while the previous batch still runs; a slot is refilled
-// only after the launch that used it completed.  Each encode is
-//   descriptors H2D, first-unit table H2D, counter := 0, persistent kernel
-// on the library's stream, ordered after the caller's stream and before it
-// again by events.  With graphs enabled the four operations are captured once
-// per slot and replayed while the batch shape (image count, work units, tile)
-// stays the same; the pointers inside the descriptors may change freely.
+// only after the launch that used it completed.  Each encode is one H2D copy
+// (descriptors, first-unit table and a zeroed work counter, one buffer) and
+// the persistent kernel, enqueued on the caller's stream.  With graphs enabled
+// the two are captured once per slot (on the library's own idle stream) and
+// the graph is launched on the caller's stream while the batch shape (image
+// count, work units, tile) stays the same; the pointers inside the
+// descriptors may change freely.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,17 +32,19 @@ using goofy_gpu::DeviceGuard;
 
 namespace {
 
+// A call's upload, one contiguous buffer: `count` descriptors (48 B each),
+// the first-unit table (4 B each) and the work counter (4 B, uploaded as 0),
+// so one copy sets up a launch.
+size_t upload_bytes(uint32_t count) { return (size_t)count * (sizeof(BatchImage) + sizeof(uint32_t)) + sizeof(uint32_t); }
+
 struct Slot {
-    BatchImage* h_desc = nullptr;
-    uint32_t* h_first = nullptr;
-    BatchImage* d_desc = nullptr;
-    uint32_t* d_first = nullptr;
-    uint32_t* d_counter = nullptr;
+    uint8_t* h_buf = nullptr;  // pinned
+    uint8_t* d_buf = nullptr;
     cudaEvent_t done = nullptr;
     bool in_flight = false;
     cudaGraphExec_t exec = nullptr;
     uint32_t g_count = 0, g_units = 0, g_ctas = 0;
-    BatchTile g_tile{0, 0, 0};
+    BatchTile g_tile{0, 0, 0, 0};
 };
 
 }  // namespace
@@ -50,10 +53,9 @@ struct goofy_gpu_batch {
     std::mutex mu;
     int device = 0;
     uint32_t max_images = 0;
-    BatchTile tile{128, 1, 256};
+    BatchTile tile{128, 1, 256, 0};
     bool graphs = true;
     cudaStream_t stream = nullptr;
-    cudaEvent_t caller_ready = nullptr;
     Slot slot[2];
     int next = 0;
     std::vector<uint32_t> units_scratch;
@@ -102,25 +104,21 @@ void free_slot(Slot& s)
 {
     if (s.done) cudaEventSynchronize(s.done);
     if (s.exec) cudaGraphExecDestroy(s.exec);
-    if (s.h_desc) cudaFreeHost(s.h_desc);
-    if (s.h_first) cudaFreeHost(s.h_first);
-    if (s.d_desc) cudaFree(s.d_desc);
-    if (s.d_first) cudaFree(s.d_first);
-    if (s.d_counter) cudaFree(s.d_counter);
+    if (s.h_buf) cudaFreeHost(s.h_buf);
+    if (s.d_buf) cudaFree(s.d_buf);
     if (s.done) cudaEventDestroy(s.done);
     s = Slot{};
 }
 
-// Enqueue H2D descriptors, counter reset and kernel on `st`.
+// Enqueue the upload (descriptors, first-unit table, zeroed counter) and the kernel on `st`.
 cudaError_t enqueue(const Slot& s, uint32_t count, uint32_t units, const BatchTile& tile, uint32_t ctas,
                     cudaStream_t st)
 {
-    cudaError_t e = cudaMemcpyAsync(s.d_desc, s.h_desc, sizeof(BatchImage) * count, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s.d_first, s.h_first, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, sizeof(uint32_t), st);
-    if (e == cudaSuccess)
-        e = goofy_gpu::launch_batch(s.d_desc, count, s.d_first, units, s.d_counter, tile, ctas, st);
+    cudaError_t e = cudaMemcpyAsync(s.d_buf, s.h_buf, upload_bytes(count), cudaMemcpyHostToDevice, st);
+    const BatchImage* d_desc = reinterpret_cast<const BatchImage*>(s.d_buf);
+    const uint32_t* d_first = reinterpret_cast<const uint32_t*>(s.d_buf + sizeof(BatchImage) * count);
+    uint32_t* d_counter = reinterpret_cast<uint32_t*>(s.d_buf + upload_bytes(count) - sizeof(uint32_t));
+    if (e == cudaSuccess) e = goofy_gpu::launch_batch(d_desc, count, d_first, units, d_counter, tile, ctas, st);
     return e;
 }
 
@@ -138,19 +136,21 @@ int encode_locked(goofy_gpu_batch* b, const goofy_gpu_image* images, uint32_t co
         s.in_flight = false;
     }
     uint32_t units = 0;
-    const int rc = validate_and_fill(images, count, tile.unit_blocks, s.h_desc, s.h_first, &units);
+    BatchImage* h_desc = reinterpret_cast<BatchImage*>(s.h_buf);
+    uint32_t* h_first = reinterpret_cast<uint32_t*>(s.h_buf + sizeof(BatchImage) * count);
+    *reinterpret_cast<uint32_t*>(s.h_buf + upload_bytes(count) - sizeof(uint32_t)) = 0;  // the work counter
+    const int rc = validate_and_fill(images, count, tile.unit_blocks, h_desc, h_first, &units);
     if (rc != GOOFY_OK) return rc;
     if (units == 0) return GOOFY_OK;
+    // warps a unit (plain) or one unit per stage of a CTA (pipeline): no more CTAs than have work
+    const uint64_t useful = tile.pipeline ? (uint64_t)units : ((uint64_t)units * 32 + tile.threads - 1) / tile.threads;
     const uint32_t ctas = (uint32_t)std::min<uint64_t>(
-        (uint64_t)goofy_gpu::batch_resident_ctas(tile.threads, tile.bpt),
-        ((uint64_t)units * 32 + tile.threads - 1) / tile.threads);
+        (uint64_t)goofy_gpu::batch_resident_ctas(tile.threads, tile.bpt, tile.pipeline), useful);
 
-    GOOFY_CUDA_TRY(cudaEventRecord(b->caller_ready, caller));
-    GOOFY_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->caller_ready, 0));
     if (b->graphs) {
         const bool match = s.exec && s.g_count == count && s.g_units == units && s.g_ctas == ctas &&
                            s.g_tile.threads == tile.threads && s.g_tile.bpt == tile.bpt &&
-                           s.g_tile.unit_blocks == tile.unit_blocks;
+                           s.g_tile.unit_blocks == tile.unit_blocks && s.g_tile.pipeline == tile.pipeline;
         if (!match) {
             if (s.exec) {
                 cudaGraphExecDestroy(s.exec);
@@ -175,14 +175,13 @@ int encode_locked(goofy_gpu_batch* b, const goofy_gpu_image* images, uint32_t co
             s.g_ctas = ctas;
             s.g_tile = tile;
         }
-        GOOFY_CUDA_TRY(cudaGraphLaunch(s.exec, b->stream));
+        GOOFY_CUDA_TRY(cudaGraphLaunch(s.exec, caller));  // (captured on the idle library stream)
     } else {
-        const cudaError_t e = enqueue(s, count, units, tile, ctas, b->stream);
+        const cudaError_t e = enqueue(s, count, units, tile, ctas, caller);
         if (e != cudaSuccess) return cuda_fail(e, "batch enqueue");
     }
-    GOOFY_CUDA_TRY(cudaEventRecord(s.done, b->stream));
+    GOOFY_CUDA_TRY(cudaEventRecord(s.done, caller));
     s.in_flight = true;
-    GOOFY_CUDA_TRY(cudaStreamWaitEvent(caller, s.done, 0));
     return GOOFY_OK;
 }
 
@@ -205,19 +204,14 @@ GOOFY_EXPORT int goofy_gpu_batch_create(goofy_gpu_batch** out, uint32_t max_imag
     b->max_images = max_images;
     auto cleanup = [&](int rc) {
         for (auto& s : b->slot) free_slot(s);
-        if (b->caller_ready) cudaEventDestroy(b->caller_ready);
         if (b->stream) cudaStreamDestroy(b->stream);
         delete b;
         return rc;
     };
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->caller_ready, cudaEventDisableTiming);
     for (auto& s : b->slot) {
-        if (e == cudaSuccess) e = cudaHostAlloc(&s.h_desc, sizeof(BatchImage) * max_images, cudaHostAllocDefault);
-        if (e == cudaSuccess) e = cudaHostAlloc(&s.h_first, sizeof(uint32_t) * max_images, cudaHostAllocDefault);
-        if (e == cudaSuccess) e = cudaMalloc(&s.d_desc, sizeof(BatchImage) * max_images);
-        if (e == cudaSuccess) e = cudaMalloc(&s.d_first, sizeof(uint32_t) * max_images);
-        if (e == cudaSuccess) e = cudaMalloc(&s.d_counter, sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaHostAlloc(&s.h_buf, upload_bytes(max_images), cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaMalloc(&s.d_buf, upload_bytes(max_images));
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
     }
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "goofy_gpu_batch_create"));
@@ -232,7 +226,6 @@ GOOFY_EXPORT void goofy_gpu_batch_destroy(goofy_gpu_batch* b)
         std::lock_guard<std::mutex> lk(b->mu);
         DeviceGuard g(b->device);
         for (auto& s : b->slot) free_slot(s);
-        if (b->caller_ready) cudaEventDestroy(b->caller_ready);
         if (b->stream) cudaStreamDestroy(b->stream);
     }
     delete b;
@@ -261,13 +254,14 @@ GOOFY_EXPORT int goofy_gpu_batch_get_tile(goofy_gpu_batch* b, goofy_gpu_batch_ti
     tile->threads_per_cta = b->tile.threads;
     tile->blocks_per_thread = b->tile.bpt;
     tile->unit_blocks = b->tile.unit_blocks;
+    tile->pipeline = b->tile.pipeline;
     return GOOFY_OK;
 }
 
 GOOFY_EXPORT int goofy_gpu_batch_set_tile(goofy_gpu_batch* b, const goofy_gpu_batch_tile* tile)
 {
     if (!b || !tile) return GOOFY_ERR_INVALID;
-    const BatchTile t{tile->threads_per_cta, tile->blocks_per_thread, tile->unit_blocks};
+    const BatchTile t{tile->threads_per_cta, tile->blocks_per_thread, tile->unit_blocks, tile->pipeline};
     if (!goofy_gpu::batch_tile_valid(t)) return GOOFY_ERR_INVALID;
     std::lock_guard<std::mutex> lk(b->mu);
     b->tile = t;
@@ -290,13 +284,18 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
     const bool graphs = b->graphs;
     b->graphs = false;  // time the launches themselves, not graph instantiation
     int rc = GOOFY_OK;
-    BatchTile best_tile{0, 0, 0};
+    BatchTile best_tile{0, 0, 0, 0};
     float best_time = 0.f;
     std::vector<float> t(reps);
-    for (uint32_t threads : {128u, 256u, 512u}) {
+    std::vector<BatchTile> candidates;
+    for (uint32_t threads : {128u, 256u, 512u})
         for (uint32_t bpt : {1u, 2u}) {
-            for (uint32_t unit : {64u, 128u, 256u, 512u, 1024u, 2048u}) {
-                const BatchTile tile{threads, bpt, unit};
+            for (uint32_t unit : {64u, 128u, 256u, 512u, 1024u, 2048u}) candidates.push_back(BatchTile{threads, bpt, unit, 0});
+            candidates.push_back(BatchTile{threads, bpt, threads * bpt, 1});  // the pipelined kernel: a unit per stage
+        }
+    for (const BatchTile& tile : candidates) {
+        {
+            {
                 if (!goofy_gpu::batch_tile_valid(tile) || rc != GOOFY_OK) continue;
                 for (uint32_t r = 0; r < reps + 1 && rc == GOOFY_OK; ++r) {
                     cudaError_t e = cudaEventRecord(ev[0], b->stream);
@@ -329,6 +328,7 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
         best->threads_per_cta = best_tile.threads;
         best->blocks_per_thread = best_tile.bpt;
         best->unit_blocks = best_tile.unit_blocks;
+        best->pipeline = best_tile.pipeline;
     }
     if (best_us) *best_us = best_time * 1e3f;
     return GOOFY_OK;

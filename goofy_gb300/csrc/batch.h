@@ -23,20 +23,31 @@ struct BatchImage {
 static_assert(sizeof(BatchImage) == 48, "BatchImage layout");
 
 struct BatchTile {
-    uint32_t threads;      // threads per CTA: 128, 256, 512
+    uint32_t threads;      // threads per CTA: 128, 256, 512 (compute threads with pipeline = 1)
     uint32_t bpt;          // blocks per lane per step: 1 or 2
-    uint32_t unit_blocks;  // blocks per work unit (multiple of 32 * bpt)
+    uint32_t unit_blocks;  // blocks per work unit (multiple of 32 * bpt; threads * bpt with pipeline = 1)
+    uint32_t pipeline;     // 0: warps pull units and load rows themselves; 1: a producer warp per CTA
+                           // bulk-copies each unit's rows into a shared-memory ring (encode_tma.cu)
 };
 
 inline bool batch_tile_valid(const BatchTile& t)
 {
     if (t.threads != 128 && t.threads != 256 && t.threads != 512) return false;
     if (t.bpt != 1 && t.bpt != 2) return false;
+    if (t.pipeline > 1) return false;
+    if (t.pipeline) return t.unit_blocks == t.threads * t.bpt;
     return t.unit_blocks >= 32 * t.bpt && t.unit_blocks <= 65536 && t.unit_blocks % (32 * t.bpt) == 0;
 }
 
 // CTAs of the batch kernel that fit on the current device at once.
-int batch_resident_ctas(uint32_t threads, uint32_t bpt);
+int batch_resident_ctas(uint32_t threads, uint32_t bpt, uint32_t pipeline = 0);
+
+// The same for the pipelined batch kernel (encode_tma.cu), and its launcher:
+// one unit of threads * bpt blocks per stage.
+int batch_tma_resident_ctas(uint32_t threads, uint32_t bpt);
+cudaError_t launch_batch_tma(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,
+                             uint32_t total_units, uint32_t* work_counter, const BatchTile& tile, uint32_t ctas,
+                             cudaStream_t stream);
 
 // Enqueue the persistent batch kernel.  `work_counter` must read 0 when the
 // kernel starts; `first_unit[i]` is images[i].first_unit (ascending, [0] = 0).

@@ -62,8 +62,9 @@ __global__ void __launch_bounds__(512) encode_batch_kernel(const BatchImage* __r
     }
 }
 
-int batch_resident_ctas(uint32_t threads, uint32_t bpt)
+int batch_resident_ctas(uint32_t threads, uint32_t bpt, uint32_t pipeline)
 {
+    if (pipeline) return batch_tma_resident_ctas(threads, bpt);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -77,6 +78,7 @@ cudaError_t launch_batch(const BatchImage* images, uint32_t n_images, const uint
                          cudaStream_t stream)
 {
     if (total_units == 0) return cudaSuccess;
+    if (tile.pipeline) return launch_batch_tma(images, n_images, first_unit, total_units, work_counter, tile, ctas, stream);
     if (tile.bpt == 1)
         encode_batch_kernel<1><<<ctas, tile.threads, 0, stream>>>(images, n_images, first_unit, total_units,
                                                                    tile.unit_blocks, work_counter);

@@ -26,6 +26,7 @@
 #include <atomic>
 
 #include "async_copy.cuh"
+#include "batch.h"
 #include "block_codec.cuh"
 #include "device_io.cuh"
 #include "kernels.h"
@@ -173,6 +174,183 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// The batch kernel on the same pipeline (tile `pipeline` = 1).  A work unit is
+// one stage: up to COMPUTE * BPT consecutive blocks of one image (they may
+// span several block rows).  CTA b takes units b, b + grid, ... (equal units
+// balance like the image kernel's tiles, and no work counter is needed); its
+// producer finds each unit's image, writes the stage's unit record and copies
+// the unit's rows: for each block row segment of nb blocks, its 4 pixel rows
+// (16 * nb bytes each) land one after another, so block k of a segment that
+// starts at unit block ks sits at 64 * ks + 16 * (k - ks) + r * 16 * nb.
+// Units of images with 4-byte aligned rows, or narrower than an eighth of a
+// unit, are not copied: their record says so and the compute warps load those
+// blocks themselves.  A record with no blocks ends the CTA's work.
+// ---------------------------------------------------------------------------
+struct UnitRec {
+    const uint8_t* src;
+    uint8_t* dst;
+    uint32_t stride, bw, bw_magic, codec;
+    uint32_t first, n;  // first block of the unit in its image, blocks in the unit (0: no more units)
+    uint32_t direct;    // 1: rows not copied (4-byte aligned source), blocks read from global memory
+    uint32_t reserved;
+};
+static_assert(sizeof(UnitRec) == 48, "UnitRec layout");
+
+constexpr size_t batch_tma_smem_bytes(const TmaLayout& l)
+{
+    return (size_t)l.stages * (l.stage_bytes + 16u + sizeof(UnitRec)) + 128u;
+}
+
+template <int BPT, int COMPUTE>
+__global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
+    encode_batch_tma(const BatchImage* __restrict__ images, uint32_t n_images, const uint32_t* __restrict__ first_unit,
+                     uint32_t total_units)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ uint32_t abort_flag;
+    constexpr uint32_t compute_warps = COMPUTE / 32;
+    constexpr TmaLayout L = tma_layout(COMPUTE, BPT);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.stages * L.stage_bytes);
+    uint64_t* empty = full + L.stages;
+    UnitRec* rec = reinterpret_cast<UnitRec*>(empty + L.stages);
+    uint8_t* ctrl_lut = reinterpret_cast<uint8_t*>(rec + L.stages);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < L.stages; ++s) {
+            mbar_init(&full[s], 1u);
+            mbar_init(&empty[s], compute_warps);
+        }
+        abort_flag = 0u;
+        mbar_init_fence();
+    }
+    fill_ctrl_lut(ctrl_lut);
+    __syncthreads();
+
+    if (warp == compute_warps) {  // producer
+        if (lane != 0) return;
+        // Units u = blockIdx.x, + gridDim.x, ...: the image of the next unit and
+        // its descriptor are looked up right after the current unit's copies are
+        // issued, while the compute warps work; the search starts at the current
+        // image (units only grow), so a batch of large images rarely searches.
+        uint32_t issued = 0, slot = 0, phase = 0;
+        uint32_t u = blockIdx.x, ii = 0;
+        BatchImage im{};
+        if (u < total_units) {
+            ii = find_image(first_unit, n_images, u);
+            im = images[ii];
+        }
+        for (;;) {
+            if (issued >= L.stages && !mbar_wait(&empty[slot], phase ^ 1u, &abort_flag, &g_pipeline_timeouts))
+                break;
+            UnitRec& r = rec[slot];
+            if (u >= total_units) {
+                r.n = 0;  // published by the arrival (release), read after the wait (acquire)
+                mbar_arrive(&full[slot]);
+                ++issued;
+                break;
+            }
+            const uint32_t first = (u - im.first_unit) * L.tile_blocks;
+            const uint32_t n = min(L.tile_blocks, im.bw * im.bh - first);
+            r.src = im.src;
+            r.dst = im.dst;
+            r.stride = im.stride;
+            r.bw = im.bw;
+            r.bw_magic = im.bw_magic;
+            r.codec = im.codec;
+            r.first = first;
+            r.n = n;
+            // narrow images would take many small copies per unit (one per pixel row of every
+            // block row): a unit is copied only when it spans at most about 9 block rows
+            const bool copy = im.vec16 && im.bw * 8u >= L.tile_blocks;
+            r.direct = copy ? 0u : 1u;
+            if (copy) {
+                mbar_arrive_expect_tx(&full[slot], 64u * n);
+                uint8_t* buf = smem + slot * L.stage_bytes;
+                for (uint32_t g = first; g < first + n;) {
+                    uint32_t bx;
+                    const uint32_t by = div_magic(g, im.bw, im.bw_magic, bx);
+                    const uint32_t nb = min(im.bw - bx, first + n - g);
+                    const uint8_t* row = im.src + (size_t)by * 4u * im.stride + 16u * (size_t)bx;
+                    uint8_t* d = buf + 64u * (g - first);
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+                        bulk_copy_g2s(d + rr * 16u * nb, row + (size_t)rr * im.stride, 16u * nb, &full[slot]);
+                    g += nb;
+                }
+            } else {
+                mbar_arrive(&full[slot]);
+            }
+            ++issued;
+            if (++slot == L.stages) {
+                slot = 0;
+                phase ^= 1u;
+            }
+            u += gridDim.x;
+            if (u < total_units && ii + 1 < n_images && first_unit[ii + 1] <= u) {
+                ii += find_image(first_unit + ii, n_images - ii, u);
+                im = images[ii];
+            }
+        }
+        if (*static_cast<volatile uint32_t*>(&abort_flag)) {
+            const uint32_t n = issued < L.stages ? issued : L.stages;
+            for (uint32_t i = issued - n; i < issued; ++i)
+                mbar_wait(&full[i % L.stages], (i / L.stages) & 1u, nullptr, &g_pipeline_timeouts);
+        }
+        return;
+    }
+
+    uint32_t slot = 0, phase = 0;
+    for (;;) {
+        if (!mbar_wait(&full[slot], phase, &abort_flag, &g_pipeline_timeouts)) break;
+        const UnitRec r = rec[slot];
+        if (r.n == 0) break;
+        const uint8_t* buf = smem + slot * L.stage_bytes;
+        uint32_t w[BPT][16];
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+            const uint32_t k = (warp * BPT + j) * 32u + lane;
+            if (k < r.n) {
+                uint32_t bx;
+                const uint32_t by = div_magic(r.first + k, r.bw, r.bw_magic, bx);
+                if (r.direct) {
+                    load_block_rows(r.src + (size_t)by * 4u * r.stride + 16u * (size_t)bx, r.stride, false, w[j]);
+                } else {
+                    const uint32_t row0 = by * r.bw;  // first block of this block row
+                    const uint32_t ks = row0 > r.first ? row0 - r.first : 0u;
+                    const uint32_t nb = min(row0 + r.bw, r.first + r.n) - max(row0, r.first);
+                    const uint8_t* p = buf + 64u * ks + 16u * (k - ks);
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr) {
+                        const uint4 v = *reinterpret_cast<const uint4*>(p + rr * 16u * nb);
+                        w[j][4 * rr + 0] = v.x;
+                        w[j][4 * rr + 1] = v.y;
+                        w[j][4 * rr + 2] = v.z;
+                        w[j][4 * rr + 3] = v.w;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+            const uint32_t k = (warp * BPT + j) * 32u + lane;
+            if (k < r.n) {
+                const uint2 e = r.codec == kBC1 ? encode_bc1(w[j]) : encode_etc1s(w[j], ctrl_lut);
+                st_stream8(r.dst + 8u * (size_t)(r.first + k), e);
+            }
+        }
+        // released only after the stores, which wait for every loaded word (see encode_image_tma)
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+        if (++slot == L.stages) {
+            slot = 0;
+            phase ^= 1u;
+        }
+    }
+}
+
 namespace {
 
 template <int CODEC, int BPT, int COMPUTE>
@@ -238,6 +416,83 @@ cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8
     } else {
         if (tile.bpt == 1) return launch_tma_bpt<kETC1S, 1>(src, stride, dst, bw, bh, tile.threads, stream);
         if (tile.bpt == 2) return launch_tma_bpt<kETC1S, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+namespace {
+
+template <int BPT, int COMPUTE>
+int batch_tma_ctas_t(int dev)
+{
+    constexpr TmaLayout L = tma_layout(COMPUTE, BPT);
+    constexpr size_t smem = batch_tma_smem_bytes(L);
+    static std::atomic<int> resident[64];
+    if (dev < 0 || dev >= 64) return 0;
+    int ctas = resident[dev].load(std::memory_order_relaxed);
+    if (ctas == 0) {
+        if (cudaFuncSetAttribute(encode_batch_tma<BPT, COMPUTE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(encode_batch_tma<BPT, COMPUTE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return 0;
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, encode_batch_tma<BPT, COMPUTE>, COMPUTE + 32,
+                                                          smem) != cudaSuccess)
+            return 0;
+        ctas = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        resident[dev].store(ctas, std::memory_order_relaxed);
+    }
+    return ctas;
+}
+
+template <int BPT, int COMPUTE>
+cudaError_t launch_batch_tma_t(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,
+                               uint32_t total_units, uint32_t* work_counter, uint32_t ctas, cudaStream_t stream)
+{
+    (void)work_counter;  // units are dealt to CTAs statically
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int resident = batch_tma_ctas_t<BPT, COMPUTE>(dev);
+    if (resident == 0) return cudaErrorInvalidValue;
+    if (ctas > (uint32_t)resident) ctas = (uint32_t)resident;
+    constexpr size_t smem = batch_tma_smem_bytes(tma_layout(COMPUTE, BPT));
+    encode_batch_tma<BPT, COMPUTE><<<ctas ? ctas : 1u, COMPUTE + 32, smem, stream>>>(images, n_images, first_unit,
+                                                                                      total_units);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int batch_tma_resident_ctas(uint32_t threads, uint32_t bpt)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    int n = 0;
+    if (bpt == 1) n = threads == 128 ? batch_tma_ctas_t<1, 128>(dev) : threads == 256 ? batch_tma_ctas_t<1, 256>(dev)
+                                                                                      : batch_tma_ctas_t<1, 512>(dev);
+    else n = threads == 128 ? batch_tma_ctas_t<2, 128>(dev) : threads == 256 ? batch_tma_ctas_t<2, 256>(dev)
+                                                                             : batch_tma_ctas_t<2, 512>(dev);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_batch_tma(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,
+                             uint32_t total_units, uint32_t* work_counter, const BatchTile& tile, uint32_t ctas,
+                             cudaStream_t stream)
+{
+    if (total_units == 0) return cudaSuccess;
+    if (tile.unit_blocks != tile.threads * tile.bpt) return cudaErrorInvalidValue;
+    const uint32_t t = tile.threads;
+    if (tile.bpt == 1) {
+        if (t == 128) return launch_batch_tma_t<1, 128>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
+        if (t == 256) return launch_batch_tma_t<1, 256>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
+        if (t == 512) return launch_batch_tma_t<1, 512>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
+    } else if (tile.bpt == 2) {
+        if (t == 128) return launch_batch_tma_t<2, 128>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
+        if (t == 256) return launch_batch_tma_t<2, 256>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
+        if (t == 512) return launch_batch_tma_t<2, 512>(images, n_images, first_unit, total_units, work_counter, ctas, stream);
     }
     return cudaErrorInvalidValue;
 }

@@ -255,9 +255,13 @@ typedef struct goofy_gpu_image {
 typedef struct goofy_gpu_batch goofy_gpu_batch;
 
 typedef struct goofy_gpu_batch_tile {
-    uint32_t threads_per_cta;   /* 128, 256, 512 */
+    uint32_t threads_per_cta;   /* 128, 256, 512 (compute threads; the pipeline adds a producer warp) */
     uint32_t blocks_per_thread; /* 1 or 2 */
-    uint32_t unit_blocks;       /* 4x4 blocks per work unit, a multiple of 32 * blocks_per_thread */
+    uint32_t unit_blocks;       /* 4x4 blocks per work unit, a multiple of 32 * blocks_per_thread;
+                                 * threads_per_cta * blocks_per_thread with pipeline = 1 */
+    uint32_t pipeline;          /* 0: warps pull work units and load their rows themselves;
+                                 * 1: per CTA a producer warp pulls units and bulk-copies their rows
+                                 *    into a shared-memory ring, compute warps encode from there */
 } goofy_gpu_batch_tile;
 
 /* A batch object for up to `max_images` images per call on `device`; owns its
@@ -267,10 +271,12 @@ int goofy_gpu_batch_create(goofy_gpu_batch** batch, uint32_t max_images, int dev
 void goofy_gpu_batch_destroy(goofy_gpu_batch* batch);
 
 /* Encode `count` images in one persistent launch: warps pull work units
- * (runs of unit_blocks blocks of one image) from a device work counter.
- * Asynchronous: ordered after the work already queued on `stream`, and later
- * work on `stream` waits for it.  Each image's output equals
- * goofy_gpu_compress_device on that image alone. */
+ * (runs of unit_blocks blocks of one image) from a device work counter, or
+ * with a pipeline tile each CTA's producer warp stages its units' rows in
+ * shared memory.  Enqueued on `stream` (one descriptor upload and the
+ * kernel, a CUDA graph replay for a repeated batch shape): ordered after the
+ * work already queued there, and later work there waits for it.  Each
+ * image's output equals goofy_gpu_compress_device on that image alone. */
 int goofy_gpu_batch_encode(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, void* stream);
 
 /* CUDA-graph replay of same-shaped batches (default on). */

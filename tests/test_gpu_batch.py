@@ -116,7 +116,8 @@ def test_graph_replay_with_new_pointers(cuda, mixed):
         b.close()
 
 
-@pytest.mark.parametrize("tile", [(128, 1, 64), (256, 2, 256), (512, 2, 2048), (512, 1, 32)])
+@pytest.mark.parametrize("tile", [(128, 1, 64), (256, 2, 256), (512, 2, 2048), (512, 1, 32),
+                                  (128, 1, 128, 1), (128, 2, 256, 1), (256, 1, 256, 1), (512, 2, 1024, 1)])
 def test_batch_tiles(cuda, mixed, tile):
     b = g.Batch(len(mixed))
     try:
@@ -156,6 +157,8 @@ def test_batch_argument_checks(cuda, mixed):
         bad[2] = 6
         assert b.encode([tuple(bad)]) == g.ERR_WIDTH
         assert b.set_tile(256, 2, 48) == g.ERR_INVALID
+        assert b.set_tile(256, 1, 512, 1) == g.ERR_INVALID  # a pipelined unit is one stage: threads * bpt
+        assert b.set_tile(256, 1, 256, 2) == g.ERR_INVALID
         assert b.encode([]) == g.OK
     finally:
         b.close()
@@ -181,14 +184,21 @@ def test_full_mixed_batch_1000_textures(cuda):
         lv["out"] = (off_out, n)
         off_in += (px.size + 255) // 256 * 256
         off_out += n
+    outs = []
     b = g.Batch(len(levels))
     try:
-        assert b.encode(descs, cuda.cuda.current_stream().cuda_stream) == g.OK, g.last_error()
-        cuda.cuda.synchronize()
-        out = arena_out.cpu().numpy()
+        for tile in (None, (512, 2, 1024, 1)):  # the default tile, then the bulk-copy pipeline
+            if tile:
+                assert b.set_tile(*tile) == g.OK
+            arena_out.zero_()
+            assert b.encode(descs, cuda.cuda.current_stream().cuda_stream) == g.OK, g.last_error()
+            cuda.cuda.synchronize()
+            outs.append(arena_out.cpu().numpy())
     finally:
         b.close()
+    assert g.pipeline_timeouts() == 0
     for lv in levels:
         o, n = lv["out"]
         want = oracle.encode(lv["codec"], lv["pixels"], lv["width"], lv["height"], threads=0 if n > 65536 else 1)
-        np.testing.assert_array_equal(out[o:o + n], want)
+        for out in outs:
+            np.testing.assert_array_equal(out[o:o + n], want)
