@@ -290,33 +290,36 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
     std::vector<BatchTile> candidates;
     for (uint32_t threads : {128u, 256u, 512u})
         for (uint32_t bpt : {1u, 2u}) {
-            for (uint32_t unit : {64u, 128u, 256u, 512u, 1024u, 2048u}) candidates.push_back(BatchTile{threads, bpt, unit, 0});
+            for (uint32_t unit : {64u, 128u, 256u, 512u, 1024u, 2048u})
+                candidates.push_back(BatchTile{threads, bpt, unit, 0});
             candidates.push_back(BatchTile{threads, bpt, threads * bpt, 1});  // the pipelined kernel: a unit per stage
         }
     for (const BatchTile& tile : candidates) {
-        {
-            {
-                if (!goofy_gpu::batch_tile_valid(tile) || rc != GOOFY_OK) continue;
-                for (uint32_t r = 0; r < reps + 1 && rc == GOOFY_OK; ++r) {
-                    cudaError_t e = cudaEventRecord(ev[0], b->stream);
-                    if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventRecord"); break; }
-                    rc = encode_locked(b, images, count, b->stream, tile);
-                    if (rc != GOOFY_OK) break;
-                    e = cudaEventRecord(ev[1], b->stream);
-                    if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-                    float ms = 0.f;
-                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
-                    if (e != cudaSuccess) { rc = cuda_fail(e, "autotune timing"); break; }
-                    if (r > 0) t[r - 1] = ms;  // the first launch is a warm-up
-                }
-                if (rc != GOOFY_OK) break;
-                std::sort(t.begin(), t.end());
-                const float med = t[reps / 2];
-                if (best_tile.threads == 0 || med < best_time) {
-                    best_time = med;
-                    best_tile = tile;
-                }
+        if (!goofy_gpu::batch_tile_valid(tile)) continue;
+        for (uint32_t r = 0; r < reps + 1 && rc == GOOFY_OK; ++r) {
+            cudaError_t e = cudaEventRecord(ev[0], b->stream);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "cudaEventRecord");
+                break;
             }
+            rc = encode_locked(b, images, count, b->stream, tile);
+            if (rc != GOOFY_OK) break;
+            e = cudaEventRecord(ev[1], b->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "autotune timing");
+                break;
+            }
+            if (r > 0) t[r - 1] = ms;  // the first launch is a warm-up
+        }
+        if (rc != GOOFY_OK) break;
+        std::sort(t.begin(), t.end());
+        const float med = t[reps / 2];
+        if (best_tile.threads == 0 || med < best_time) {
+            best_time = med;
+            best_tile = tile;
         }
     }
     b->graphs = graphs;
