@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=4.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
-    p.add_argument("--profile", choices=["encode", "quality", "mips", "batch"],
+    p.add_argument("--profile", choices=["encode", "quality", "mips", "batch", "batch-pipeline"],
                    help="only run a few launches of one kernel family (for ncu captures) and exit")
     p.add_argument("--profile-size", type=int, default=4096, help="image side for --profile")
     return p.parse_args()
@@ -850,6 +850,27 @@ def run_profile(args):
 
     lib_build.build()
     assert g.init(0) == g.OK, g.last_error()
+    if args.profile == "batch-pipeline":  # 16 textures of 2048x2048 (8 per codec), the pipelined tile, three launches
+        side, n = 2048, 16
+        img = workloads.scene(side, side, 3, threads=0)
+        keep, descs = [], []
+        for i in range(n):
+            src = torch.from_numpy(img.reshape(-1)).cuda()
+            out = torch.empty(g.out_size(side, side), dtype=torch.uint8, device="cuda")
+            keep += [src, out]
+            descs.append((src.data_ptr(), out.data_ptr(), side, side, 4 * side, i % 2))
+        b = g.Batch(n)
+        try:
+            assert b.set_tile(512, 2, 1024, 1) == g.OK
+            arr = g.images_array(descs)
+            for _ in range(3):
+                assert b.encode(arr, torch.cuda.current_stream().cuda_stream) == g.OK, g.last_error()
+            torch.cuda.synchronize()
+        finally:
+            b.close()
+        print(json.dumps({"profile": "batch-pipeline", "textures": n, "side": side,
+                          "pipeline_timeouts": g.pipeline_timeouts()}))
+        return 0
     if args.profile == "batch":  # the mixed batch of --batch-textures textures, three launches, default tile
         levels = workloads.texture_batch(args.batch_textures)
         keep, descs = [], []
