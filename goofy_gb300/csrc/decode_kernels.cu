@@ -22,6 +22,10 @@
 
 namespace goofy_gpu {
 
+// Threads per CTA of every decoding kernel: the palette column stride, a
+// constant so that a pixel's palette address is a shift and an add.
+constexpr uint32_t kDecodeThreads = 256;
+
 __device__ __forceinline__ uint2 load_block8(const uint8_t* p)
 {
     uint2 v;
@@ -30,19 +34,19 @@ __device__ __forceinline__ uint2 load_block8(const uint8_t* p)
 }
 
 template <int CODEC>
-__global__ void __launch_bounds__(256) decode_image_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
+__global__ void __launch_bounds__(kDecodeThreads) decode_image_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
                                                            uint32_t nblk, uint8_t* __restrict__ rgba, size_t stride,
                                                            unsigned long long* __restrict__ unsupported)
 {
     pdl_launch_dependents();
-    __shared__ uint32_t pal[8 * 256];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t pal[8 * kDecodeThreads];
+    const uint32_t i = blockIdx.x * kDecodeThreads + threadIdx.x;
     bool ok = true;
     pdl_wait();
     if (i < nblk) {
         const uint32_t by = i / bw, bx = i - by * bw;
         uint32_t px[16];
-        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), pal + threadIdx.x, blockDim.x, px);
+        ok = decode_block<CODEC>(load_block8(blocks + 8u * (size_t)i), pal + threadIdx.x, kDecodeThreads, px);
         uint8_t* row = rgba + (size_t)by * 4u * stride + 16u * (size_t)bx;
 #pragma unroll
         for (int y = 0; y < 4; ++y)
@@ -100,20 +104,20 @@ __device__ __forceinline__ uint32_t luma_row(const uint32_t (&a)[4], const uint3
 // sums, then the CTA reduces (shuffles, shared memory) and adds its six
 // totals with one atomic each.
 template <int CODEC>
-__global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
+__global__ void __launch_bounds__(kDecodeThreads) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
                                                           uint32_t nblk, const uint8_t* __restrict__ src,
                                                           size_t stride, bool vec16,
                                                           unsigned long long* __restrict__ sums)
 {
     pdl_launch_dependents();
-    __shared__ uint32_t pal[8 * 256];
+    __shared__ uint32_t pal[8 * kDecodeThreads];
     unsigned long long s[6] = {0, 0, 0, 0, 0, 0};
     const uint32_t bw_magic = 0xffffffffu / bw;
     pdl_wait();
     // software pipeline: the next block's source rows and code are loaded
     // before this block is decoded and compared
-    const uint32_t step = gridDim.x * blockDim.x;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t step = gridDim.x * kDecodeThreads;
+    uint32_t i = blockIdx.x * kDecodeThreads + threadIdx.x;
     uint32_t w[16];
     uint2 blk = make_uint2(0, 0);
     if (i < nblk) {
@@ -133,7 +137,7 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
             load_block_rows(src + (size_t)by * 4u * stride + 16u * (size_t)bx, stride, vec16, w);
             blk = load_block8(blocks + 8u * (size_t)(i + step));
         }
-        const bool ok = decode_block<CODEC>(cur_blk, pal + threadIdx.x, blockDim.x, px);
+        const bool ok = decode_block<CODEC>(cur_blk, pal + threadIdx.x, kDecodeThreads, px);
         uint32_t acc[4] = {0, 0, 0, 0};  // one block: at most 16 * 255^2 per channel
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
@@ -157,7 +161,7 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
     __syncthreads();
     if (threadIdx.x < 6) {
         unsigned long long t = 0;
-        for (uint32_t k = 0; k < (blockDim.x >> 5); ++k) t += part[threadIdx.x][k];
+        for (uint32_t k = 0; k < (kDecodeThreads >> 5); ++k) t += part[threadIdx.x][k];
         if (t) atomicAdd(&sums[threadIdx.x], t);
     }
 }
@@ -167,13 +171,13 @@ __global__ void __launch_bounds__(256) block_error_kernel(const uint8_t* __restr
 // encoder's batch kernel, decode the image's blocks (`dst`) and compare them
 // with its source; a warp sums its unit and adds six totals to the image's
 // sums[6 * image + c].
-__global__ void __launch_bounds__(256) quality_batch_kernel(const BatchImage* __restrict__ images, uint32_t n_images,
+__global__ void __launch_bounds__(kDecodeThreads) quality_batch_kernel(const BatchImage* __restrict__ images, uint32_t n_images,
                                                             const uint32_t* __restrict__ first_unit,
                                                             uint32_t total_units, uint32_t unit_blocks,
                                                             uint32_t* __restrict__ work_counter,
                                                             unsigned long long* __restrict__ sums)
 {
-    __shared__ uint32_t pal[8 * 256];
+    __shared__ uint32_t pal[8 * kDecodeThreads];
     const uint32_t lane = threadIdx.x & 31u;
     for (;;) {
         uint32_t u = 0;
@@ -191,8 +195,8 @@ __global__ void __launch_bounds__(256) quality_batch_kernel(const BatchImage* __
             const uint32_t by = div_magic(b, im.bw, im.bw_magic, bx);
             uint32_t px[16], w[16];
             const uint2 blk = load_block8(im.dst + 8u * (size_t)b);
-            const bool ok = im.codec == kBC1 ? decode_block<kBC1>(blk, pal + threadIdx.x, blockDim.x, px)
-                                             : decode_block<kETC1S>(blk, pal + threadIdx.x, blockDim.x, px);
+            const bool ok = im.codec == kBC1 ? decode_block<kBC1>(blk, pal + threadIdx.x, kDecodeThreads, px)
+                                             : decode_block<kETC1S>(blk, pal + threadIdx.x, kDecodeThreads, px);
             load_block_rows(im.src + (size_t)by * 4u * im.stride + 16u * (size_t)bx, im.stride, im.vec16 != 0, w);
 #pragma unroll
             for (int y = 0; y < 4; ++y) {
@@ -226,7 +230,7 @@ cudaError_t launch_quality_batch(const BatchImage* images, uint32_t n_images, co
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t warps = total_units, ctas = (warps + 7) / 8;
     const uint32_t grid = (uint32_t)(ctas < (uint64_t)sms * 8u ? ctas : (uint64_t)sms * 8u);
-    quality_batch_kernel<<<grid, 256, 0, stream>>>(images, n_images, first_unit, total_units, unit_blocks,
+    quality_batch_kernel<<<grid, kDecodeThreads, 0, stream>>>(images, n_images, first_unit, total_units, unit_blocks,
                                                    work_counter, sums);
     return cudaGetLastError();
 }
@@ -236,11 +240,11 @@ cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint
 {
     const uint32_t bw = width / 4, nblk = bw * (height / 4);
     if (nblk == 0) return cudaSuccess;
-    const uint32_t grid = (nblk + 255) / 256;
+    const uint32_t grid = (nblk + kDecodeThreads - 1) / kDecodeThreads;
     if (codec == kBC1)
-        return launch_pdl(decode_image_kernel<kBC1>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, rgba, stride,
+        return launch_pdl(decode_image_kernel<kBC1>, dim3(grid), dim3(kDecodeThreads), 0, stream, blocks, bw, nblk, rgba, stride,
                           unsupported);
-    return launch_pdl(decode_image_kernel<kETC1S>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, rgba, stride,
+    return launch_pdl(decode_image_kernel<kETC1S>, dim3(grid), dim3(kDecodeThreads), 0, stream, blocks, bw, nblk, rgba, stride,
                       unsupported);
 }
 
@@ -252,11 +256,11 @@ cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t grid = min((nblk + 255) / 256, (uint32_t)(sms > 0 ? sms : 1) * 8u);
+    const uint32_t grid = min((nblk + kDecodeThreads - 1) / kDecodeThreads, (uint32_t)(sms > 0 ? sms : 1) * 8u);
     if (codec == kBC1)
-        return launch_pdl(block_error_kernel<kBC1>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, src, stride,
+        return launch_pdl(block_error_kernel<kBC1>, dim3(grid), dim3(kDecodeThreads), 0, stream, blocks, bw, nblk, src, stride,
                           vec16, sums);
-    return launch_pdl(block_error_kernel<kETC1S>, dim3(grid), dim3(256), 0, stream, blocks, bw, nblk, src, stride,
+    return launch_pdl(block_error_kernel<kETC1S>, dim3(grid), dim3(kDecodeThreads), 0, stream, blocks, bw, nblk, src, stride,
                       vec16, sums);
 }
 
