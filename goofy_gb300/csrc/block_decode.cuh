@@ -136,8 +136,15 @@ GOOFY_FN bool decode_block(uint2 blk, uint32_t* store, uint32_t stride, uint32_t
             for (int k = 0; k < 4; ++k) store[(4 + k) * stride] = ok ? pal[k] : 0u;
         }
         const uint32_t codes = etc1_codes(w1);
+        if (one) {  // every block this encoder writes: one palette, no sub-block offsets
+#pragma unroll
+            for (int y = 0; y < 4; ++y)
+#pragma unroll
+                for (int x = 0; x < 4; ++x) px[4 * y + x] = store[((codes >> (2 * (4 * x + y))) & 3u) * stride];
+            return ok;
+        }
         // sub-block 1: right half (x >= 2) without flip, bottom half (y >= 2) with flip
-        const uint32_t s1 = one ? 0u : 4u * stride;
+        const uint32_t s1 = 4u * stride;
         const uint32_t lower_right = s1, upper_right = flip ? 0u : s1, lower_left = flip ? s1 : 0u;
 #pragma unroll
         for (int y = 0; y < 4; ++y)
