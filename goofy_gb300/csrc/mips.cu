@@ -104,7 +104,9 @@ __device__ __forceinline__ void mip_tile(const uint4 (&r)[4], bool act, uint32_t
         buf[0][(y3 << w3_log2) + x3] = v3;
     }
     uint32_t cw_log2 = w3_log2, ch_log2 = h3_log2;
-    for (uint32_t l = 3; l < nlev; ++l) {
+#pragma unroll
+    for (uint32_t l = 3; l < 6; ++l) {  // unrolled: the level indexes `out` as a constant (no stack copy)
+        if (l >= nlev) break;
         __syncthreads();
         const uint32_t* in = buf[(l - 3) & 1];
         uint32_t* next = buf[(l - 2) & 1];
