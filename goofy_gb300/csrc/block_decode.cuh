@@ -121,6 +121,23 @@ GOOFY_FN bool decode_block(uint2 blk, uint32_t* store, uint32_t stride, uint32_t
     } else {
         // the block is big-endian: bytes 0..3 of blk.x are bits 63..32
         const uint32_t w0 = perm(blk.x, 0u, 0x0123u), w1 = perm(blk.y, 0u, 0x0123u);
+        if ((w0 & 0x07070702u) == 0x00000002u && ((w0 >> 5) & 7u) == ((w0 >> 2) & 7u)) {
+            // ETC1s shape (every block this encoder writes): differential, zero deltas, one
+            // table.  Both sub-blocks have the 5-bit colour (bits 31..27, 23..19, 15..11)
+            // expanded by bit replication as base: one palette, no sub-block offsets.
+            const uint32_t c5 = (w0 >> 3) & 0x1f1f1f00u;  // R5, G5, B5 in bytes 3, 2, 1
+            const uint32_t e = ((c5 << 3) & 0xf8f8f800u) | ((c5 >> 2) & 0x07070700u);
+            uint32_t pal[4];
+            etc1_subpalette(perm(e, 0u, 0x4123u), (w0 >> 5) & 7u, pal);  // bytes R, G, B, 0
+#pragma unroll
+            for (int k = 0; k < 4; ++k) store[k * stride] = pal[k];
+            const uint32_t codes = etc1_codes(w1);
+#pragma unroll
+            for (int y = 0; y < 4; ++y)
+#pragma unroll
+                for (int x = 0; x < 4; ++x) px[4 * y + x] = store[((codes >> (2 * (4 * x + y))) & 3u) * stride];
+            return true;
+        }
         const bool flip = w0 & 1u;
         uint32_t b0, b1, pal[4];
         const bool ok = etc1_bases(w0, b0, b1);
