@@ -91,6 +91,31 @@ def test_decoder_random_blocks_vs_oracle(emu, codec):
         assert 0 < bad < (w // 4) * (h // 4)
 
 
+def test_decoder_etc1s_shaped_blocks_vs_oracle(emu):
+    """Random ETC1s-shaped blocks (differential mode, zero deltas, one table
+    for both halves, either flip) take the decoder's fast path; individual-
+    mode blocks with equal halves and differential blocks with a non-zero
+    delta or two tables take the general one.  All equal the oracle."""
+    rng = np.random.default_rng(23)
+    w, h = 256, 256
+    n = (w // 4) * (h // 4)
+    c5 = rng.integers(0, 32, (n, 3))
+    table = rng.integers(0, 8, n)
+    kind = np.arange(n) % 4  # 0, 1: ETC1s-shaped; 2: a non-zero delta; 3: two tables
+    delta = np.where(kind[:, None] == 2, rng.integers(1, 8, (n, 3)), 0)
+    table2 = np.where(kind == 3, (table + 1 + rng.integers(0, 7, n)) % 8, table)
+    flip = rng.integers(0, 2, n)
+    w0 = ((c5[:, 0] << 27) | (delta[:, 0] << 24) | (c5[:, 1] << 19) | (delta[:, 1] << 16) | (c5[:, 2] << 11) |
+          (delta[:, 2] << 8) | (table << 5) | (table2 << 2) | 2 | flip).astype(np.uint64)
+    w1 = rng.integers(0, 1 << 32, n, dtype=np.uint64)
+    be = ((w0 << np.uint64(32)) | w1).astype(">u8")  # the block's 8 bytes, big-endian
+    blocks = np.frombuffer(be.tobytes(), np.uint8).copy()
+    got, bad = _decode(emu, 1, blocks, w, h)
+    want, want_bad = oracle.decode(1, blocks, w, h)
+    np.testing.assert_array_equal(got, want)
+    assert bad == want_bad
+
+
 @pytest.mark.parametrize("name,codec", [("bc1", 0), ("etc1s", 1)])
 def test_decoder_on_encoder_output(emu, golden, name, codec):
     w, h = int(golden["kat_width"]), int(golden["kat_height"])
