@@ -245,6 +245,34 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
 
 
+def run_dropin_latency(g, img, sides=(256, 1024, 4096), calls=50):
+    """Wall time of one goofy::compressDXT1 / compressETC1 call (the drop-in
+    entry points, synchronous, host buffers) as a caller of the reference sees
+    it: contiguous numpy (pageable) copies of the scene's top-left corner,
+    median of `calls` calls after five untimed ones."""
+    import numpy as np
+
+    res = {}
+    for side in sides:
+        src = np.ascontiguousarray(img[:side, :4 * side])
+        out = np.empty(g.out_size(side, side), np.uint8)
+        row = {}
+        for name, fn in (("bc1", g.compressDXT1), ("etc1s", g.compressETC1)):
+            for _ in range(5):
+                if fn(out, src, side, side, 4 * side) != 0:
+                    raise RuntimeError(g.last_error())
+            ts = []
+            for _ in range(calls):
+                t0 = time.perf_counter()
+                fn(out, src, side, side, 4 * side)
+                ts.append(time.perf_counter() - t0)
+            row[name] = round(1e6 * statistics.median(ts), 1)
+        res["%dx%d" % (side, side)] = row
+    res["note"] = ("median wall time of one drop-in call from Python (ctypes) with pageable numpy buffers, "
+                   "%d calls per entry; it includes a kernel launch and a stream synchronisation" % calls)
+    return res
+
+
 def run_pair(args, g, torch, src, dst, codecs, stream, device):
     """The timed step's two images (BC1 of one copy, ETC1s of the other) in
     one batch launch instead of two image launches: the bandwidth-bound BC1
@@ -746,13 +774,15 @@ def run_gpu(args):
             page_out = np.empty(n_out, np.uint8)
             e2e_rate(page_out.ctypes.data, page_in.ctypes.data, 1)
             pageable_e2e = e2e_rate(page_out.ctypes.data, page_in.ctypes.data, e2e_steps)
+            dropin = run_dropin_latency(g, img) if world == 1 else None
             e2e = {"value": round(value_e2e, 1), "unit": "MPix/s",
                    "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * n_out, "steps": e2e_steps,
                    "api": "goofy_gpu_compress_host (the engine of goofy::compressDXT1/ETC1), pinned host in/out, "
                           "default path selection (direct: the kernel reads / writes the host buffers over "
                           "NVLink-C2C)",
                    "staged_path_mpix_s": round(staged_e2e, 1), "pageable_buffers_mpix_s": round(pageable_e2e, 1),
-                   "host_link_bound_mpix_s": "about 52700 (measured H2D ceiling ~211 GB/s at 4 B/px)"}
+                   "host_link_bound_mpix_s": "about 52700 (measured H2D ceiling ~211 GB/s at 4 B/px)",
+                   "dropin_call_us": dropin}
         finally:
             g.host_free(p_in)
             g.host_free(p_out)

@@ -44,6 +44,39 @@ def test_roofline_traffic_comes_from_the_committed_profiles():
     assert bench.read_traffic("no_such_kernel") is None
 
 
+def test_dropin_latency_calls_each_entry_point_on_contiguous_corners():
+    """The drop-in timing passes each entry point a contiguous copy of the
+    image's top-left side x side corner with the drop-in's own arguments."""
+    import numpy as np
+
+    seen = []
+
+    class FakeLib:
+        def out_size(self, w, h):
+            return w * h // 2
+
+        def _call(self, name, out, src, w, h, stride):
+            assert src.flags.c_contiguous and src.shape == (h, 4 * w) and stride == 4 * w
+            assert out.size == w * h // 2 and src[0, 0] == 7
+            seen.append((name, w))
+            return 0
+
+        def compressDXT1(self, *a):
+            return self._call("bc1", *a)
+
+        def compressETC1(self, *a):
+            return self._call("etc1s", *a)
+
+        def last_error(self):
+            return ""
+
+    img = np.full((512, 2048), 7, np.uint8)
+    res = bench.run_dropin_latency(FakeLib(), img, sides=(64, 512), calls=4)
+    assert set(res) == {"64x64", "512x512", "note"}
+    assert all(set(res[k]) == {"bc1", "etc1s"} and min(res[k].values()) >= 0 for k in ("64x64", "512x512"))
+    assert len(seen) == 2 * 2 * (5 + 4) and {s for _, s in seen} == {64, 512}
+
+
 def test_peak_is_the_measured_copy_bandwidth():
     peak, kind = bench.read_peaks()
     path = os.path.join(bench.ROOT, "MEASURED_PEAKS.json")
