@@ -19,6 +19,8 @@ previous launch did not touch (inputs larger than the 129 MB L2).
                 is recorded between two launches of a timed loop: one there
                 delays the next launch's start by a few microseconds.
 * cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
+* both_codecs_one_pass -- beside the headline: the same two outputs from one
+                read of the image (goofy_gpu_compress_both_*), device and host.
 
 ``--impl reference`` times the reference's CPU implementation of the path on
 this host's cores instead (the reference compiled from its own sources where
@@ -60,7 +62,7 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=4.0, help="length of each offered-load run")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
-    p.add_argument("--profile", choices=["encode", "quality", "mips", "batch", "batch-pipeline"],
+    p.add_argument("--profile", choices=["encode", "quality", "mips", "batch", "batch-pipeline", "both"],
                    help="only run a few launches of one kernel family (for ncu captures) and exit")
     p.add_argument("--profile-size", type=int, default=4096, help="image side for --profile")
     return p.parse_args()
@@ -303,6 +305,73 @@ def run_pair(args, g, torch, src, dst, codecs, stream, device):
             "ms_per_step": round(ms, 4), "mpix_s": round(px / (ms / 1e3) / 1e6, 1),
             "hbm_gbs": round(ALG_BYTES_PER_PX * px / (ms / 1e3) / 1e9, 1), "tile": tile,
             "bit_exact_vs_image_kernels": all(bool(torch.equal(outs[c], dst[c])) for c in codecs)}
+
+
+def run_both(args, g, torch, img, src, dst, codecs, stream):
+    """The two-codec pass (goofy_gpu_compress_both_*): BC1 and ETC1s blocks of
+    the 8192x8192 scene from one read of it.  Device: K launches back to back
+    between two events, inputs alternating between the two 256 MiB copies and
+    outputs between two buffers; 5 algorithmic B/px (4 read, 0.5 + 0.5
+    written).  Host: the same through the synchronous host call from pinned
+    buffers, copies over the host link inside the region.  Both checked
+    bit-exact against the single-codec outputs of the timed step."""
+    import ctypes
+
+    import numpy as np
+
+    sh = stream.cuda_stream
+    n = g.out_size(W, H)
+    outs = [torch.empty(2 * n, dtype=torch.uint8, device=src[0].device) for _ in range(2)]
+
+    def launch(k):
+        o = outs[k % 2].data_ptr()
+        rc = g.compress_both_device(o, o + n, src[k % 2].data_ptr(), W, H, 4 * W, sh)
+        if rc != g.OK:
+            raise RuntimeError("compress_both_device: %s %s" % (g.status_string(rc), g.last_error()))
+
+    for k in range(4):
+        launch(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        launch(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    exact = all(bool(torch.equal(outs[k][:n], dst[codecs[0]]) and torch.equal(outs[k][n:], dst[codecs[1]]))
+                for k in range(2))
+    res = {"api": "goofy_gpu_compress_both_device: BC1 + ETC1s blocks of one image from one read of it",
+           "tile": list(g.get_tile(g.CODEC_BOTH)), "mean_launch_us": round(1e3 * ms, 2),
+           "image_mpix_s": round(W * H / (ms / 1e3) / 1e6, 1),
+           "codec_mpix_s": round(2 * W * H / (ms / 1e3) / 1e6, 1),
+           "hbm_gbs": round(5.0 * W * H / (ms / 1e3) / 1e9, 1), "algorithmic_bytes_per_px": 5.0,
+           "bit_exact_vs_single_codec": exact}
+    if args.no_e2e:
+        return res
+    nbytes = img.size
+    p_in, p_out = g.host_alloc(nbytes), g.host_alloc(2 * n)
+    try:
+        np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p_in))[:] = img.reshape(-1)
+        for _ in range(2):
+            assert g.compress_both_host(p_out, p_out + n, p_in, W, H, 4 * W) == g.OK, g.last_error()
+        steps = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            rc = g.compress_both_host(p_out, p_out + n, p_in, W, H, 4 * W)
+            if rc != g.OK:
+                raise RuntimeError(g.last_error())
+        dt = (time.perf_counter() - t0) / steps
+        host = np.ctypeslib.as_array((ctypes.c_uint8 * (2 * n)).from_address(p_out))
+        exact_host = bool(np.array_equal(host[:n], dst[codecs[0]].cpu().numpy()) and
+                          np.array_equal(host[n:], dst[codecs[1]].cpu().numpy()))
+    finally:
+        g.host_free(p_in)
+        g.host_free(p_out)
+    res["e2e"] = {"api": "goofy_gpu_compress_both_host, pinned host in/out (direct path)", "steps": steps,
+                  "ms_per_call": round(1e3 * dt, 3), "codec_mpix_s": round(2 * W * H / dt / 1e6, 1),
+                  "h2d_bytes_per_call": nbytes, "d2h_bytes_per_call": 2 * n, "bit_exact": exact_host}
+    return res
 
 
 def run_two_streams(args, g, torch, src, dst, codecs, stream):
@@ -839,6 +908,7 @@ def run_gpu(args):
     mips = run_mips(g, torch, workloads, img, src[0], stream) if single else None
     pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
     two_streams = run_two_streams(args, g, torch, src, dst, codecs, stream) if single else None
+    both = run_both(args, g, torch, img, src, dst, codecs, stream) if single else None
     batched = None
     if not args.no_batched and single:
         batched = run_batched(args, g, torch, stream, dev)
@@ -857,7 +927,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "both_codecs_one_pass": both, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
@@ -929,6 +999,9 @@ def run_profile(args):
     for c in (g.CODEC_BC1, g.CODEC_ETC1S):
         for _ in range(3 if args.profile == "encode" else 1):
             assert g.compress_device(c, dst[c].data_ptr(), src.data_ptr(), n, n, 4 * n, sh) == g.OK, g.last_error()
+    if args.profile == "both":
+        for _ in range(3):
+            assert g.compress_both_device(dst[0], dst[1], src, n, n, 4 * n, sh) == g.OK, g.last_error()
     if args.profile == "quality":
         sums = torch.zeros(6, dtype=torch.int64, device="cuda")
         rgba = torch.empty(n * n * 4, dtype=torch.uint8, device="cuda")

@@ -35,6 +35,7 @@ ERR_TOO_LARGE = -10
 
 CODEC_BC1 = 0
 CODEC_ETC1S = 1
+CODEC_BOTH = 2  # the two-codec pass: compress_both_*, and its tile in get_tile / set_tile
 NOALLOC_MAX_IMAGES = 256
 CODECS = {"bc1": CODEC_BC1, "dxt1": CODEC_BC1, "etc1s": CODEC_ETC1S, "etc1": CODEC_ETC1S}
 
@@ -115,6 +116,8 @@ def _declare(lib):
         "goofy_gpu_compress_host": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32]),
         "goofy_gpu_compress_bc1_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
         "goofy_gpu_compress_etc1s_host": (ctypes.c_int, [_VP, _VP, _U32, _U32, _U32]),
+        "goofy_gpu_compress_both_device": (ctypes.c_int, [_VP, _VP, _VP, _U32, _U32, _U32, _VP]),
+        "goofy_gpu_compress_both_host": (ctypes.c_int, [_VP, _VP, _VP, _U32, _U32, _U32]),
         "goofy_gpu_host_alloc": (_VP, [ctypes.c_size_t]),
         "goofy_gpu_set_host_path": (ctypes.c_int, [ctypes.c_int]),
         "goofy_gpu_get_host_path": (ctypes.c_int, []),
@@ -248,6 +251,18 @@ def compress_host(codec, dst, src, width, height, stride):
 def compress_device(codec, dst, src, width, height, stride, stream=None):
     """Device pointers (ints or torch tensors); `stream` is a cudaStream_t handle (int) or None."""
     return lib().goofy_gpu_compress_device(codec, _addr(dst), _addr(src), width, height, stride, stream)
+
+
+def compress_both_device(dst_bc1, dst_etc1s, src, width, height, stride, stream=None):
+    """BC1 and ETC1s blocks of one device image from one pass over it (device
+    pointers or torch tensors), each bit-identical to its single-codec call."""
+    return lib().goofy_gpu_compress_both_device(_addr(dst_bc1), _addr(dst_etc1s), _addr(src), width, height, stride,
+                                                stream)
+
+
+def compress_both_host(dst_bc1, dst_etc1s, src, width, height, stride):
+    """The same from host buffers, synchronous (the drop-in's host paths)."""
+    return lib().goofy_gpu_compress_both_host(_addr(dst_bc1), _addr(dst_etc1s), _addr(src), width, height, stride)
 
 
 def init(device=0):

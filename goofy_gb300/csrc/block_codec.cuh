@@ -34,7 +34,7 @@
 
 namespace goofy_gpu {
 
-enum Codec : int { kBC1 = 0, kETC1S = 1 };
+enum Codec : int { kBC1 = 0, kETC1S = 1, kBoth = 2 };  // kBoth: one pass writing both codecs' blocks
 
 #if !defined(GOOFY_HOST_EMULATION)
 GOOFY_FN uint32_t perm(uint32_t a, uint32_t b, uint32_t sel) { return __byte_perm(a, b, sel); }
@@ -121,21 +121,47 @@ GOOFY_FN BlockRange block_range(uint32_t mn_rb, uint32_t mn_g, uint32_t mx_rb, u
     return r;
 }
 
+// Channel extents of a block: R/B lane words (R in bits 0-7, B in bits
+// 16-23) and words whose byte 0 is the minimum / maximum G.
+struct Extents {
+    uint32_t mn_rb, mx_rb, mn_g, mx_g;
+};
+
+// Lane words of one block shared by the extents and the ETC1s mean tree:
+// rb[i] = R, B of pixel i; gp[2y + x] = G(y, x), G(y, x + 2).
+struct BlockLanes {
+    uint32_t rb[16], gp[8];
+};
+
+GOOFY_FN void block_lanes(const uint32_t (&w)[16], BlockLanes& l)
+{
+#pragma unroll
+    for (int i = 0; i < 16; ++i) l.rb[i] = w[i] & 0x00ff00ffu;
+#pragma unroll
+    for (int y = 0; y < 4; ++y)
+#pragma unroll
+        for (int x = 0; x < 2; ++x)  // lanes G(y, x), G(y, x+2): byte dot products and a multiply-add (FMA pipe)
+            l.gp[2 * y + x] = __dp4a(w[4 * y + x + 2], 0x00000100u, 0u) * 0x10000u + __dp4a(w[4 * y + x], 0x00000100u, 0u);
+}
+
+GOOFY_FN Extents lane_extents(const BlockLanes& l)
+{
+    Extents e;
+    e.mn_rb = tree_min<16>(l.rb);
+    e.mx_rb = tree_max<16>(l.rb);
+    const uint32_t mn_g = tree_min<8>(l.gp), mx_g = tree_max<8>(l.gp);
+    e.mn_g = vmin2(mn_g, mn_g >> 16);
+    e.mx_g = vmax2(mx_g, mx_g >> 16);
+    return e;
+}
+
 // ---------------------------------------------------------------------------
 // BC1: returns {c0 | c1 << 16, indices}; pixel i (row-major) at bits 2i..2i+1.
 // goofy_tc.h:1276-1357.
 // ---------------------------------------------------------------------------
-GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
+GOOFY_FN uint2 bc1_from_extents(const uint32_t (&w)[16], const Extents& e)
 {
-    uint32_t rb[16], gg[8];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) rb[i] = w[i] & 0x00ff00ffu;           // lanes R, B
-#pragma unroll
-    for (int k = 0; k < 8; ++k) gg[k] = perm(w[k], w[k + 8], 0x5511u);  // lanes 257*G of two pixels
-    const uint32_t mn_rb = tree_min<16>(rb), mx_rb = tree_max<16>(rb);
-    uint32_t mn_g = tree_min<8>(gg), mx_g = tree_max<8>(gg);
-    mn_g = vmin2(mn_g, mn_g >> 16);  // byte 0 = min G
-    mx_g = vmax2(mx_g, mx_g >> 16);
+    const uint32_t mn_rb = e.mn_rb, mx_rb = e.mx_rb, mn_g = e.mn_g, mx_g = e.mx_g;
     const BlockRange br = block_range(mn_rb, mn_g, mx_rb, mx_g);
 
     // thresholds on S of two pixels at once (16-bit lanes): flag bits 14 / 15
@@ -160,26 +186,33 @@ GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
     return make_uint2(ends, idx);
 }
 
+GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
+{
+    uint32_t rb[16], gg[8];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) rb[i] = w[i] & 0x00ff00ffu;           // lanes R, B
+#pragma unroll
+    for (int k = 0; k < 8; ++k) gg[k] = perm(w[k], w[k + 8], 0x5511u);  // lanes 257*G of two pixels
+    Extents e;
+    e.mn_rb = tree_min<16>(rb);
+    e.mx_rb = tree_max<16>(rb);
+    const uint32_t mn_g = tree_min<8>(gg), mx_g = tree_max<8>(gg);
+    e.mn_g = vmin2(mn_g, mn_g >> 16);  // byte 0 = min G
+    e.mx_g = vmax2(mx_g, mx_g >> 16);
+    return bc1_from_extents(w, e);
+}
+
 // ---------------------------------------------------------------------------
 // ETC1s: returns {word0, word1} as the reference stores them (little-endian
 // u32s of the big-endian ETC1 block).  goofy_tc.h:1358-1493.
 // `ctrl_lut` holds etc_control_byte(2*i) for i < 128.
 // ---------------------------------------------------------------------------
-GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
+GOOFY_FN uint2 etc1s_from_extents(const uint32_t (&w)[16], const BlockLanes& l, const Extents& e,
+                                  const uint8_t* ctrl_lut)
 {
-    uint32_t rb[16], gp[8];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) rb[i] = w[i] & 0x00ff00ffu;
-#pragma unroll
-    for (int y = 0; y < 4; ++y)
-#pragma unroll
-        for (int x = 0; x < 2; ++x)  // lanes G(y, x), G(y, x+2): byte dot products and a multiply-add (FMA pipe)
-            gp[2 * y + x] = __dp4a(w[4 * y + x + 2], 0x00000100u, 0u) * 0x10000u + __dp4a(w[4 * y + x], 0x00000100u, 0u);
-    const uint32_t mn_rb = tree_min<16>(rb), mx_rb = tree_max<16>(rb);
-    uint32_t mn_g = tree_min<8>(gp), mx_g = tree_max<8>(gp);
-    mn_g = vmin2(mn_g, mn_g >> 16);
-    mx_g = vmax2(mx_g, mx_g >> 16);
-    const BlockRange br = block_range(mn_rb, mn_g, mx_rb, mx_g);
+    const uint32_t(&rb)[16] = l.rb;
+    const uint32_t(&gp)[8] = l.gp;
+    const BlockRange br = block_range(e.mn_rb, e.mn_g, e.mx_rb, e.mx_g);
 
     // block mean, rounding-average tree kept exact at scale 2^level
     uint32_t col_rb[4];
@@ -252,6 +285,25 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
         }
     const uint32_t word1 = group[0] + (group[1] >> 5) + (group[2] >> 10) + (group[3] >> 11);
     return make_uint2(word0, word1);
+}
+
+GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
+{
+    BlockLanes l;
+    block_lanes(w, l);
+    return etc1s_from_extents(w, l, lane_extents(l), ctrl_lut);
+}
+
+// Both codecs from one set of lanes and extents: the R/B masks, the min / max
+// trees, the brightness statistics and the per-pixel luma sums are computed
+// once.  {BC1 block, ETC1s block}, each bit-identical to its own encoder's.
+GOOFY_FN uint4 encode_both(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
+{
+    BlockLanes l;
+    block_lanes(w, l);
+    const Extents e = lane_extents(l);
+    const uint2 a = bc1_from_extents(w, e), b = etc1s_from_extents(w, l, e, ctrl_lut);
+    return make_uint4(a.x, a.y, b.x, b.y);
 }
 
 template <int CODEC>

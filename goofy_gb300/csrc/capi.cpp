@@ -55,13 +55,14 @@ using goofy_gpu::Tile;
 
 #define CUDA_TRY GOOFY_CUDA_TRY
 
-Tile g_tile[2] = {{128, 2, 0}, {512, 2, 2}};  // BC1: register-loading grid, ETC1s: bulk-copy pipeline; 2 blocks a thread
+// BC1: register-loading grid; ETC1s and the two-codec pass: bulk-copy pipeline; 2 blocks a thread
+Tile g_tile[3] = {{128, 2, 0}, {512, 2, 2}, {512, 2, 2}};
 std::mutex g_tile_mu;
 
 Tile tile_for(int codec)
 {
     std::lock_guard<std::mutex> lk(g_tile_mu);
-    return g_tile[codec & 1];
+    return g_tile[codec == GOOFY_CODEC_BOTH ? 2 : codec & 1];
 }
 
 struct Buffer {
@@ -193,10 +194,15 @@ int check_args(int codec, const void* dst, const void* src, uint32_t width, uint
 
 constexpr size_t kBandBytes = 16u << 20;  // source bytes per band of the host path
 
-int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height, uint32_t stride)
+// Either codec into `dst`, or (codec GOOFY_CODEC_BOTH) the BC1 blocks into
+// `dst` and the ETC1s blocks into `dst2` from one pass.
+int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height, uint32_t stride,
+                       uint8_t* dst2 = nullptr)
 {
-    int rc = check_args(codec, dst, src, width, height, stride);
+    const bool both = codec == GOOFY_CODEC_BOTH;
+    int rc = check_args(both ? GOOFY_CODEC_BC1 : codec, dst, src, width, height, stride);
     if (rc <= 0) return rc;
+    if (both && !dst2) return GOOFY_ERR_INVALID;
     HostPath& hp = host_path();
     std::lock_guard<std::mutex> lk(hp.mu);
     if (!hp.ready) {
@@ -212,15 +218,18 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
     if (path != GOOFY_HOST_PATH_STAGED) {
         const void* dsrc = device_view(src, hp.pageable_ok);
         void* ddst = const_cast<void*>(device_view(dst, hp.pageable_ok));
+        void* ddst2 = both ? const_cast<void*>(device_view(dst2, hp.pageable_ok)) : nullptr;
         const uintptr_t sa = reinterpret_cast<uintptr_t>(dsrc);
-        const bool aligned = sa % 4 == 0 && stride % 4 == 0 && reinterpret_cast<uintptr_t>(ddst) % 8 == 0;
-        if (dsrc && ddst && aligned) {
+        const bool aligned = sa % 4 == 0 && stride % 4 == 0 && reinterpret_cast<uintptr_t>(ddst) % 8 == 0 &&
+                             reinterpret_cast<uintptr_t>(ddst2) % 8 == 0;
+        if (dsrc && ddst && (!both || ddst2) && aligned) {
             const SrcAccess access = (sa % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
             // bulk async copies only ever read device memory: host rows go through the register-loading kernel
             Tile t = tile_for(codec);
             if (t.persistent == 2) t.persistent = 0;
             CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(dsrc), stride,
-                                             static_cast<uint8_t*>(ddst), width, height, t, access, hp.stream[0]));
+                                             static_cast<uint8_t*>(ddst), width, height, t, access, hp.stream[0],
+                                             static_cast<uint8_t*>(ddst2)));
             CUDA_TRY(cudaStreamSynchronize(hp.stream[0]));
             return GOOFY_OK;
         }
@@ -233,16 +242,19 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
     const size_t dpitch = (row_bytes + 15) & ~size_t(15);  // device / staging pitch: 16-byte rows
     const uint32_t band_bh = (uint32_t)std::max<size_t>(1, std::min<size_t>(bh, kBandBytes / (4 * dpitch)));
     const uint32_t nbands = (bh + band_bh - 1) / band_bh;
-    const bool src_pinned = is_pinned(src), dst_pinned = is_pinned(dst);
+    const bool src_pinned = is_pinned(src), dst_pinned = is_pinned(dst) && (!both || is_pinned(dst2));
+    // output planes of a band slot: BC1 or ETC1s at 0, and the ETC1s blocks of the two-codec pass at band_out
     const size_t band_in = (size_t)band_bh * 4 * dpitch, band_out = (size_t)band_bh * bw * 8;
+    const size_t slot_out = both ? 2 * band_out : band_out;
     const int slots = nbands > 1 ? 2 : 1;
     for (int s = 0; s < slots; ++s) {
         if ((rc = hp.ensure_device(hp.d_src[s], band_in)) != GOOFY_OK) return rc;
-        if ((rc = hp.ensure_device(hp.d_dst[s], band_out)) != GOOFY_OK) return rc;
+        if ((rc = hp.ensure_device(hp.d_dst[s], slot_out)) != GOOFY_OK) return rc;
         if (!src_pinned && (rc = hp.ensure_pinned(hp.h_src[s], band_in)) != GOOFY_OK) return rc;
-        if (!dst_pinned && (rc = hp.ensure_pinned(hp.h_dst[s], band_out)) != GOOFY_OK) return rc;
+        if (!dst_pinned && (rc = hp.ensure_pinned(hp.h_dst[s], slot_out)) != GOOFY_OK) return rc;
     }
     const Tile tile = tile_for(codec);
+    uint8_t* const planes[2] = {dst, dst2};
 
     // band b: rows [b*band_bh, ...); slot b % slots.  A slot is reused only
     // after its previous band finished (and, for pageable dst, was copied out).
@@ -251,7 +263,9 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
         CUDA_TRY(cudaEventSynchronize(hp.done[s]));
         if (!dst_pinned) {
             const uint32_t rows = std::min(band_bh, bh - b * band_bh);
-            std::memcpy(dst + (size_t)b * band_bh * bw * 8, hp.h_dst[s].p, (size_t)rows * bw * 8);
+            for (int k = 0; k < (both ? 2 : 1); ++k)
+                std::memcpy(planes[k] + (size_t)b * band_bh * bw * 8, hp.h_dst[s].p + k * band_out,
+                            (size_t)rows * bw * 8);
         }
         return GOOFY_OK;
     };
@@ -270,9 +284,12 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
             CUDA_TRY(cudaMemcpyAsync(hp.d_src[s].p, stage, (size_t)rows * 4 * dpitch, cudaMemcpyHostToDevice, st));
         }
         CUDA_TRY(goofy_gpu::launch_image(codec, hp.d_src[s].p, dpitch, hp.d_dst[s].p, width, rows * 4, tile,
-                                         SrcAccess::kVec16, st));
-        uint8_t* out = dst_pinned ? dst + (size_t)b * band_bh * bw * 8 : hp.h_dst[s].p;
-        CUDA_TRY(cudaMemcpyAsync(out, hp.d_dst[s].p, (size_t)rows * bw * 8, cudaMemcpyDeviceToHost, st));
+                                         SrcAccess::kVec16, st, both ? hp.d_dst[s].p + band_out : nullptr));
+        for (int k = 0; k < (both ? 2 : 1); ++k) {
+            uint8_t* out = dst_pinned ? planes[k] + (size_t)b * band_bh * bw * 8 : hp.h_dst[s].p + k * band_out;
+            CUDA_TRY(cudaMemcpyAsync(out, hp.d_dst[s].p + k * band_out, (size_t)rows * bw * 8,
+                                     cudaMemcpyDeviceToHost, st));
+        }
         CUDA_TRY(cudaEventRecord(hp.done[s], st));
     }
     for (uint32_t b = nbands > (uint32_t)slots ? nbands - slots : 0; b < nbands; ++b)
@@ -293,6 +310,25 @@ int compress_device_impl(int codec, void* dst, const void* src, uint32_t width, 
     else return GOOFY_ERR_ALIGNMENT;
     CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
                                      width, height, tile_for(codec), access, static_cast<cudaStream_t>(stream)));
+    return GOOFY_OK;
+}
+
+int compress_both_device_impl(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width, uint32_t height,
+                              uint32_t stride, void* stream)
+{
+    int rc = check_args(GOOFY_CODEC_BC1, dst_bc1, src, width, height, stride);
+    if (rc <= 0) return rc;
+    if (!dst_etc1s) return GOOFY_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(dst_bc1) % 8 != 0 || reinterpret_cast<uintptr_t>(dst_etc1s) % 8 != 0)
+        return GOOFY_ERR_ALIGNMENT;
+    const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+    SrcAccess access;
+    if (s % 16 == 0 && stride % 16 == 0) access = SrcAccess::kVec16;
+    else if (s % 4 == 0 && stride % 4 == 0) access = SrcAccess::kWord4;
+    else return GOOFY_ERR_ALIGNMENT;
+    CUDA_TRY(goofy_gpu::launch_image(GOOFY_CODEC_BOTH, static_cast<const uint8_t*>(src), stride,
+                                     static_cast<uint8_t*>(dst_bc1), width, height, tile_for(GOOFY_CODEC_BOTH), access,
+                                     static_cast<cudaStream_t>(stream), static_cast<uint8_t*>(dst_etc1s)));
     return GOOFY_OK;
 }
 
@@ -358,6 +394,18 @@ GOOFY_EXPORT int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t*
     return compress_host_impl(codec, dst, src, width, height, stride);
 }
 
+GOOFY_EXPORT int goofy_gpu_compress_both_device(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width,
+                                                uint32_t height, uint32_t stride, void* stream)
+{
+    return compress_both_device_impl(dst_bc1, dst_etc1s, src, width, height, stride, stream);
+}
+
+GOOFY_EXPORT int goofy_gpu_compress_both_host(uint8_t* dst_bc1, uint8_t* dst_etc1s, const uint8_t* src,
+                                              uint32_t width, uint32_t height, uint32_t stride)
+{
+    return compress_host_impl(GOOFY_CODEC_BOTH, dst_bc1, src, width, height, stride, dst_etc1s);
+}
+
 GOOFY_EXPORT int goofy_gpu_compress_bc1_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                                              uint32_t stride)
 {
@@ -397,7 +445,7 @@ GOOFY_EXPORT void goofy_gpu_host_free(void* p)
 
 GOOFY_EXPORT int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile)
 {
-    if (!tile || (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S)) return GOOFY_ERR_INVALID;
+    if (!tile || codec < GOOFY_CODEC_BC1 || codec > GOOFY_CODEC_BOTH) return GOOFY_ERR_INVALID;
     const Tile t = tile_for(codec);
     tile->threads_per_cta = t.threads;
     tile->blocks_per_thread = t.bpt;
@@ -407,9 +455,9 @@ GOOFY_EXPORT int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile)
 
 GOOFY_EXPORT int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile)
 {
-    if (!tile || (codec != GOOFY_CODEC_BC1 && codec != GOOFY_CODEC_ETC1S)) return GOOFY_ERR_INVALID;
+    if (!tile || codec < GOOFY_CODEC_BC1 || codec > GOOFY_CODEC_BOTH) return GOOFY_ERR_INVALID;
     const Tile t{tile->threads_per_cta, tile->blocks_per_thread, tile->persistent};
-    if (!goofy_gpu::tile_valid(t)) return GOOFY_ERR_INVALID;
+    if (!goofy_gpu::tile_valid(t) || (codec == GOOFY_CODEC_BOTH && t.bpt > 2)) return GOOFY_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_tile_mu);
     g_tile[codec] = t;
     return GOOFY_OK;

@@ -54,14 +54,22 @@ __device__ __forceinline__ Segment load_segment(const uint8_t* __restrict__ src,
 }
 
 template <int CODEC, int BPT>
-__device__ __forceinline__ void encode_segment(uint8_t* __restrict__ dst, uint32_t bw, Segment sg,
-                                               const uint32_t (&w)[BPT][16], const uint8_t* ctrl_lut)
+__device__ __forceinline__ void encode_segment(uint8_t* __restrict__ dst, uint8_t* __restrict__ dst2, uint32_t bw,
+                                               Segment sg, const uint32_t (&w)[BPT][16], const uint8_t* ctrl_lut)
 {
-    uint8_t* out = dst + (size_t)sg.by * bw * 8u;
+    const size_t row = (size_t)sg.by * bw * 8u;
 #pragma unroll
     for (int j = 0; j < BPT; ++j) {
         const uint32_t bx = sg.bx0 + 32u * j;
-        if (bx < bw) st_stream8(out + 8u * (size_t)bx, encode_block<CODEC>(w[j], ctrl_lut));
+        if (bx < bw) {
+            if constexpr (CODEC == kBoth) {
+                const uint4 e = encode_both(w[j], ctrl_lut);
+                st_stream8(dst + row + 8u * (size_t)bx, make_uint2(e.x, e.y));
+                st_stream8(dst2 + row + 8u * (size_t)bx, make_uint2(e.z, e.w));
+            } else {
+                st_stream8(dst + row + 8u * (size_t)bx, encode_block<CODEC>(w[j], ctrl_lut));
+            }
+        }
     }
 }
 
@@ -71,13 +79,13 @@ __device__ __forceinline__ void encode_segment(uint8_t* __restrict__ dst, uint32
 // One segment per warp: every lane issues its 4*BPT row loads up front.
 template <int CODEC, int BPT, SrcAccess ACCESS>
 __global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __restrict__ src, size_t stride,
-                                                           uint8_t* __restrict__ dst, uint32_t bw,
-                                                           uint32_t total_segs, uint32_t segs_per_row,
+                                                           uint8_t* __restrict__ dst, uint8_t* __restrict__ dst2,
+                                                           uint32_t bw, uint32_t total_segs, uint32_t segs_per_row,
                                                            uint32_t seg_magic)
 {
     pdl_launch_dependents();
     __shared__ uint8_t ctrl_lut[128];
-    if constexpr (CODEC == kETC1S) {
+    if constexpr (CODEC != kBC1) {
         fill_ctrl_lut(ctrl_lut);
         __syncthreads();
     }
@@ -86,7 +94,7 @@ __global__ void __launch_bounds__(512) encode_image_kernel(const uint8_t* __rest
     pdl_wait();
     uint32_t w[BPT][16];
     const Segment sg = load_segment<BPT, ACCESS>(src, stride, bw, seg, segs_per_row, seg_magic, threadIdx.x & 31u, w);
-    encode_segment<CODEC, BPT>(dst, bw, sg, w, ctrl_lut);
+    encode_segment<CODEC, BPT>(dst, dst2, bw, sg, w, ctrl_lut);
 }
 
 template <int CODEC, int BPT, SrcAccess ACCESS>
@@ -111,12 +119,12 @@ __global__ void __launch_bounds__(512) encode_image_persistent(const uint8_t* __
     while (seg < total_segs) {
         uint32_t next = seg + warp_stride;
         if (next < total_segs) sb = load_segment<BPT, ACCESS>(src, stride, bw, next, segs_per_row, seg_magic, lane, b);
-        encode_segment<CODEC, BPT>(dst, bw, sa, a, ctrl_lut);
+        encode_segment<CODEC, BPT>(dst, nullptr, bw, sa, a, ctrl_lut);
         seg = next;
         if (seg >= total_segs) break;
         next = seg + warp_stride;
         if (next < total_segs) sa = load_segment<BPT, ACCESS>(src, stride, bw, next, segs_per_row, seg_magic, lane, a);
-        encode_segment<CODEC, BPT>(dst, bw, sb, b, ctrl_lut);
+        encode_segment<CODEC, BPT>(dst, nullptr, bw, sb, b, ctrl_lut);
         seg = next;
     }
 }
@@ -157,18 +165,19 @@ static void prefer_shared(K kernel, int slot)
 }
 
 template <int CODEC, int BPT, SrcAccess ACCESS>
-static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uint8_t* dst2, uint32_t bw, uint32_t bh,
                             uint32_t threads, bool persistent, cudaStream_t stream)
 {
+    constexpr bool kHasPersistent = BPT <= 2 && CODEC != kBoth;
     prefer_shared(encode_image_kernel<CODEC, BPT, ACCESS>, 0);
-    if constexpr (BPT <= 2) prefer_shared(encode_image_persistent<CODEC, BPT, ACCESS>, 1);
+    if constexpr (kHasPersistent) prefer_shared(encode_image_persistent<CODEC, BPT, ACCESS>, 1);
     const uint32_t segs = (bw + 32u * BPT - 1) / (32u * BPT);
     const uint64_t total = (uint64_t)segs * bh;
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;
     const uint32_t wpc = threads / 32u;
     uint64_t ctas = (total + wpc - 1) / wpc;
     const uint32_t magic = 0xffffffffu / segs;
-    if constexpr (BPT <= 2) {
+    if constexpr (kHasPersistent) {
         if (persistent) {
             const uint64_t resident = (uint64_t)resident_ctas<CODEC, BPT, ACCESS>(threads);
             if (ctas > resident) ctas = resident;
@@ -177,41 +186,47 @@ static cudaError_t launch_t(const uint8_t* src, size_t stride, uint8_t* dst, uin
         }
     }
     return launch_pdl(encode_image_kernel<CODEC, BPT, ACCESS>, dim3((unsigned)ctas), dim3(threads), 0, stream, src,
-                      stride, dst, bw, (uint32_t)total, segs, magic);
+                      stride, dst, dst2, bw, (uint32_t)total, segs, magic);
 }
 
 template <int CODEC, SrcAccess ACCESS>
-static cudaError_t launch_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh, Tile tile,
-                              cudaStream_t stream)
+static cudaError_t launch_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint8_t* dst2, uint32_t bw,
+                              uint32_t bh, Tile tile, cudaStream_t stream)
 {
     switch (tile.bpt) {
-    case 1: return launch_t<CODEC, 1, ACCESS>(src, stride, dst, bw, bh, tile.threads, tile.persistent, stream);
-    case 2: return launch_t<CODEC, 2, ACCESS>(src, stride, dst, bw, bh, tile.threads, tile.persistent, stream);
-    case 4: return launch_t<CODEC, 4, ACCESS>(src, stride, dst, bw, bh, tile.threads, false, stream);
+    case 1: return launch_t<CODEC, 1, ACCESS>(src, stride, dst, dst2, bw, bh, tile.threads, tile.persistent, stream);
+    case 2: return launch_t<CODEC, 2, ACCESS>(src, stride, dst, dst2, bw, bh, tile.threads, tile.persistent, stream);
+    case 4:
+        if constexpr (CODEC != kBoth) return launch_t<CODEC, 4, ACCESS>(src, stride, dst, dst2, bw, bh, tile.threads, false, stream);
+        return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
     }
 }
 
 template <int CODEC>
-static cudaError_t launch_access(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
-                                 Tile tile, SrcAccess access, cudaStream_t stream)
+static cudaError_t launch_access(const uint8_t* src, size_t stride, uint8_t* dst, uint8_t* dst2, uint32_t bw,
+                                 uint32_t bh, Tile tile, SrcAccess access, cudaStream_t stream)
 {
-    if (access == SrcAccess::kVec16) return launch_bpt<CODEC, SrcAccess::kVec16>(src, stride, dst, bw, bh, tile, stream);
-    return launch_bpt<CODEC, SrcAccess::kWord4>(src, stride, dst, bw, bh, tile, stream);
+    if (access == SrcAccess::kVec16)
+        return launch_bpt<CODEC, SrcAccess::kVec16>(src, stride, dst, dst2, bw, bh, tile, stream);
+    return launch_bpt<CODEC, SrcAccess::kWord4>(src, stride, dst, dst2, bw, bh, tile, stream);
 }
 
 cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
-                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream)
+                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream, uint8_t* dst2)
 {
     if (!tile_valid(tile)) return cudaErrorInvalidValue;
+    if (codec != kBC1 && codec != kETC1S && (codec != kBoth || !dst2)) return cudaErrorInvalidValue;
     const uint32_t bw = width / 4, bh = height / 4;
     if (bw == 0 || bh == 0) return cudaSuccess;
     if (tile.persistent == 2) {
-        if (access == SrcAccess::kVec16) return launch_image_tma(codec, src, stride, dst, width, height, tile, stream);
+        if (access == SrcAccess::kVec16)
+            return launch_image_tma(codec, src, stride, dst, width, height, tile, stream, dst2);
         tile.persistent = 0;  // word-aligned rows: the register-loading kernel with the same shape
     }
-    if (codec == kBC1) return launch_access<kBC1>(src, stride, dst, bw, bh, tile, access, stream);
-    return launch_access<kETC1S>(src, stride, dst, bw, bh, tile, access, stream);
+    if (codec == kBC1) return launch_access<kBC1>(src, stride, dst, nullptr, bw, bh, tile, access, stream);
+    if (codec == kETC1S) return launch_access<kETC1S>(src, stride, dst, nullptr, bw, bh, tile, access, stream);
+    return launch_access<kBoth>(src, stride, dst, dst2, bw, bh, tile, access, stream);
 }
 
 }  // namespace goofy_gpu

@@ -72,8 +72,9 @@ constexpr size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * 
 
 template <int CODEC, int BPT, int COMPUTE>
 __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
-    encode_image_tma(const uint8_t* __restrict__ src, size_t stride, uint8_t* __restrict__ dst, uint32_t bw,
-                     uint32_t tiles_per_row, uint32_t total_tiles, uint32_t tile_magic)
+    encode_image_tma(const uint8_t* __restrict__ src, size_t stride, uint8_t* __restrict__ dst,
+                     uint8_t* __restrict__ dst2, uint32_t bw, uint32_t tiles_per_row, uint32_t total_tiles,
+                     uint32_t tile_magic)
 {
     pdl_launch_dependents();
     extern __shared__ __align__(128) uint8_t smem[];
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
         abort_flag = 0u;
         mbar_init_fence();
     }
-    if constexpr (CODEC == kETC1S) fill_ctrl_lut(ctrl_lut);
+    if constexpr (CODEC != kBC1) fill_ctrl_lut(ctrl_lut);
     __syncthreads();
     pdl_wait();  // no global memory before the previous kernel in the stream is done
 
@@ -151,11 +152,19 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
                 }
             }
         }
-        uint8_t* out = dst + ((size_t)by * bw + bx0) * 8u;
+        const size_t o = ((size_t)by * bw + bx0) * 8u;
 #pragma unroll
         for (int j = 0; j < BPT; ++j) {
             const uint32_t b = (warp * BPT + j) * 32u + lane;
-            if (b < nb) st_stream8(out + 8u * (size_t)b, encode_block<CODEC>(w[j], ctrl_lut));
+            if (b < nb) {
+                if constexpr (CODEC == kBoth) {
+                    const uint4 e = encode_both(w[j], ctrl_lut);
+                    st_stream8(dst + o + 8u * (size_t)b, make_uint2(e.x, e.y));
+                    st_stream8(dst2 + o + 8u * (size_t)b, make_uint2(e.z, e.w));
+                } else {
+                    st_stream8(dst + o + 8u * (size_t)b, encode_block<CODEC>(w[j], ctrl_lut));
+                }
+            }
         }
         // Release the stage only now.  An arrival right after the shared loads
         // can overtake them: the loads wait in the load/store queue (behind
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
 namespace {
 
 template <int CODEC, int BPT, int COMPUTE>
-cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint8_t* dst2, uint32_t bw, uint32_t bh,
                          cudaStream_t stream)
 {
     constexpr TmaLayout L = tma_layout(COMPUTE, BPT);
@@ -387,17 +396,17 @@ cudaError_t launch_tma_t(const uint8_t* src, size_t stride, uint8_t* dst, uint32
     if (total > 0x7fffffffull) return cudaErrorInvalidValue;
     const uint32_t grid = (uint32_t)(total < (uint64_t)ctas ? total : (uint64_t)ctas);
     return launch_pdl(encode_image_tma<CODEC, BPT, COMPUTE>, dim3(grid), dim3(block), smem, stream, src, stride, dst,
-                      bw, tiles_per_row, (uint32_t)total, 0xffffffffu / tiles_per_row);
+                      dst2, bw, tiles_per_row, (uint32_t)total, 0xffffffffu / tiles_per_row);
 }
 
 template <int CODEC, int BPT>
-cudaError_t launch_tma_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint32_t bw, uint32_t bh,
+cudaError_t launch_tma_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint8_t* dst2, uint32_t bw, uint32_t bh,
                            uint32_t threads, cudaStream_t stream)
 {
     switch (threads) {
-    case 128: return launch_tma_t<CODEC, BPT, 128>(src, stride, dst, bw, bh, stream);
-    case 256: return launch_tma_t<CODEC, BPT, 256>(src, stride, dst, bw, bh, stream);
-    case 512: return launch_tma_t<CODEC, BPT, 512>(src, stride, dst, bw, bh, stream);
+    case 128: return launch_tma_t<CODEC, BPT, 128>(src, stride, dst, dst2, bw, bh, stream);
+    case 256: return launch_tma_t<CODEC, BPT, 256>(src, stride, dst, dst2, bw, bh, stream);
+    case 512: return launch_tma_t<CODEC, BPT, 512>(src, stride, dst, dst2, bw, bh, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -405,17 +414,20 @@ cudaError_t launch_tma_bpt(const uint8_t* src, size_t stride, uint8_t* dst, uint
 }  // namespace
 
 cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
-                             uint32_t height, Tile tile, cudaStream_t stream)
+                             uint32_t height, Tile tile, cudaStream_t stream, uint8_t* dst2)
 {
     const uint32_t bw = width / 4, bh = height / 4;
     if (bw == 0 || bh == 0) return cudaSuccess;
     if (reinterpret_cast<uintptr_t>(src) % 16 || stride % 16) return cudaErrorInvalidValue;
     if (codec == kBC1) {
-        if (tile.bpt == 1) return launch_tma_bpt<kBC1, 1>(src, stride, dst, bw, bh, tile.threads, stream);
-        if (tile.bpt == 2) return launch_tma_bpt<kBC1, 2>(src, stride, dst, bw, bh, tile.threads, stream);
-    } else {
-        if (tile.bpt == 1) return launch_tma_bpt<kETC1S, 1>(src, stride, dst, bw, bh, tile.threads, stream);
-        if (tile.bpt == 2) return launch_tma_bpt<kETC1S, 2>(src, stride, dst, bw, bh, tile.threads, stream);
+        if (tile.bpt == 1) return launch_tma_bpt<kBC1, 1>(src, stride, dst, nullptr, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_bpt<kBC1, 2>(src, stride, dst, nullptr, bw, bh, tile.threads, stream);
+    } else if (codec == kETC1S) {
+        if (tile.bpt == 1) return launch_tma_bpt<kETC1S, 1>(src, stride, dst, nullptr, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_bpt<kETC1S, 2>(src, stride, dst, nullptr, bw, bh, tile.threads, stream);
+    } else if (codec == kBoth && dst2) {
+        if (tile.bpt == 1) return launch_tma_bpt<kBoth, 1>(src, stride, dst, dst2, bw, bh, tile.threads, stream);
+        if (tile.bpt == 2) return launch_tma_bpt<kBoth, 2>(src, stride, dst, dst2, bw, bh, tile.threads, stream);
     }
     return cudaErrorInvalidValue;
 }

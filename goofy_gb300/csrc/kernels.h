@@ -29,14 +29,17 @@ enum class SrcAccess : int {
 };
 
 // Encode a whole image (width, height multiples of 4) into row-major 8-byte
-// blocks at `dst`.  Only enqueues; returns the launch error, if any.
+// blocks at `dst`.  Only enqueues; returns the launch error, if any.  With
+// codec kBoth (block_codec.cuh) one pass writes the BC1 blocks to `dst` and
+// the ETC1s blocks to `dst2` (shapes: 1 or 2 blocks a thread; a resident
+// grid with prefetch runs as the plain grid).
 cudaError_t launch_image(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
-                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream);
+                         uint32_t height, Tile tile, SrcAccess access, cudaStream_t stream, uint8_t* dst2 = nullptr);
 
 // The bulk-copy pipeline kernel (tile.persistent == 2); needs a 16-byte
 // aligned source base and stride.
 cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8_t* dst, uint32_t width,
-                             uint32_t height, Tile tile, cudaStream_t stream);
+                             uint32_t height, Tile tile, cudaStream_t stream, uint8_t* dst2 = nullptr);
 
 // Pipeline waits that gave up on the current device since the last reset.
 cudaError_t pipeline_timeouts(unsigned int* count, bool reset);

@@ -34,6 +34,8 @@ extern "C" {
 
 #define GOOFY_CODEC_BC1 0   /* DXT1 / BC1, goofySimdEncode<GOOFY_DXT1> */
 #define GOOFY_CODEC_ETC1S 1 /* ETC1s, goofySimdEncode<GOOFY_ETC1> */
+#define GOOFY_CODEC_BOTH 2  /* both from one read of the image: goofy_gpu_compress_both_*, and the
+                             * tile of that pass in goofy_gpu_{get,set}_tile only */
 
 /* ---- library -------------------------------------------------------------- */
 
@@ -91,6 +93,23 @@ int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src, uint32_t wid
 int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                             uint32_t stride);
 
+/* ---- both codecs from one read of the image -------------------------------- */
+
+/* The BC1 blocks of goofy::compressDXT1 into `dst_bc1` and the ETC1s blocks
+ * of goofy::compressETC1 into `dst_etc1s` ((width/4)(height/4)*8 bytes each),
+ * bit-identical to the two single-codec calls, from one pass over `src`: the
+ * image is read once (4 B/px instead of the two calls' 8; 1 B/px written
+ * either way) and the per-block work both encoders share (channel extents, brightness range,
+ * per-pixel luma sums) is done once.  No reference counterpart: the reference
+ * harness calls the two encoders one after the other on every image
+ * (Src/main.cpp:925-929).  Same rules as the single-codec calls; the two
+ * outputs must not overlap.  Device form: async on `stream`, with the tile of
+ * GOOFY_CODEC_BOTH.  Host form: synchronous, pinned or pageable buffers. */
+int goofy_gpu_compress_both_device(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width,
+                                   uint32_t height, uint32_t stride, void* stream);
+int goofy_gpu_compress_both_host(uint8_t* dst_bc1, uint8_t* dst_etc1s, const uint8_t* src, uint32_t width,
+                                 uint32_t height, uint32_t stride);
+
 /* How the host-pointer entry points move data (process-wide setting):
  * AUTO (default): DIRECT when both buffers are GPU-accessible -- pinned
  * memory, or any host memory where the GPU walks the host page tables
@@ -118,7 +137,9 @@ typedef struct goofy_gpu_tile {
                                  *    thread; 16-byte aligned sources, others run shape 0) */
 } goofy_gpu_tile;
 
-/* Get / set the tile the image kernels launch with, per codec. */
+/* Get / set the tile the image kernels launch with, per codec
+ * (GOOFY_CODEC_BOTH: the two-codec pass; 1 or 2 blocks a thread, and mode 1
+ * runs as mode 0 there). */
 int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile);
 int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
 

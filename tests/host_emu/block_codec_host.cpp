@@ -8,6 +8,8 @@
 #include "block_codec.cuh"
 #include "block_decode.cuh"
 
+// codec 0: BC1, 1: ETC1s, 2: both from encode_both (BC1 blocks at `out`, the
+// ETC1s blocks right after them).
 extern "C" int host_emu_encode(int codec, uint8_t* out, const uint8_t* src, unsigned width, unsigned height,
                                unsigned stride)
 {
@@ -20,9 +22,19 @@ extern "C" int host_emu_encode(int codec, uint8_t* out, const uint8_t* src, unsi
             uint32_t w[16];
             for (int y = 0; y < 4; ++y)
                 std::memcpy(&w[4 * y], src + (size_t)(4 * by + y) * stride + 16 * (size_t)bx, 16);
-            uint2 r = codec == 0 ? goofy_gpu::encode_bc1(w) : goofy_gpu::encode_etc1s(w, lut);
-            std::memcpy(out + 8 * ((size_t)by * bw + bx), &r.x, 4);
-            std::memcpy(out + 8 * ((size_t)by * bw + bx) + 4, &r.y, 4);
+            uint8_t* o = out + 8 * ((size_t)by * bw + bx);
+            if (codec == 2) {
+                const uint4 r = goofy_gpu::encode_both(w, lut);
+                uint8_t* o2 = o + 8 * (size_t)bw * bh;
+                std::memcpy(o, &r.x, 4);
+                std::memcpy(o + 4, &r.y, 4);
+                std::memcpy(o2, &r.z, 4);
+                std::memcpy(o2 + 4, &r.w, 4);
+                continue;
+            }
+            const uint2 r = codec == 0 ? goofy_gpu::encode_bc1(w) : goofy_gpu::encode_etc1s(w, lut);
+            std::memcpy(o, &r.x, 4);
+            std::memcpy(o + 4, &r.y, 4);
         }
     return 0;
 }

@@ -70,6 +70,34 @@ def test_edge_blocks_vs_oracle(emu):
         np.testing.assert_array_equal(_encode(emu, codec, img, w, h), oracle.encode(codec, img, w, h))
 
 
+def _encode_both(emu, img, w, h):
+    n = (w // 4) * (h // 4) * 8
+    out = np.zeros(2 * n, np.uint8)
+    assert emu.host_emu_encode(2, out.ctypes.data, img.ctypes.data, w, h, img.strides[0]) == 0
+    return out[:n], out[n:]
+
+
+def test_both_codecs_in_one_pass(emu, golden):
+    """encode_both (shared lanes, extents and luma sums) gives each codec's
+    own blocks: golden vectors, random blocks of every spread and the edge
+    cases of the oracle tests."""
+    w, h = int(golden["kat_width"]), int(golden["kat_height"])
+    bc1, etc = _encode_both(emu, golden["kat_input"], w, h)
+    np.testing.assert_array_equal(bc1, golden["kat_bc1"])
+    np.testing.assert_array_equal(etc, golden["kat_etc1s"])
+    for key, img in (("cfg0", workloads.scene(256, 256, 0)), ("stress", workloads.stress(256, 256, 2))):
+        bc1, etc = _encode_both(emu, img, 256, 256)
+        np.testing.assert_array_equal(bc1, golden[key + "_bc1"])
+        np.testing.assert_array_equal(etc, golden[key + "_etc1s"])
+    rng = np.random.default_rng(9)
+    for amp in (255, 40, 6, 1, 0):
+        img = rng.integers(0, 256, (64, 4 * 128)).astype(np.int64)
+        img = np.clip(img - img % 64 + rng.integers(-amp, amp + 1, img.shape), 0, 255).astype(np.uint8)
+        bc1, etc = _encode_both(emu, img, 128, 64)
+        np.testing.assert_array_equal(bc1, oracle.encode(0, img, 128, 64))
+        np.testing.assert_array_equal(etc, oracle.encode(1, img, 128, 64))
+
+
 def _decode(emu, codec, blocks, w, h):
     img = np.zeros((h, 4 * w), np.uint8)
     bad = emu.host_emu_decode(codec, np.ascontiguousarray(blocks).ctypes.data, w, h, img.ctypes.data, 4 * w)

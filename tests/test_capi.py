@@ -66,6 +66,25 @@ def test_c_abi_argument_checks(built):
     assert lib.goofy_gpu_status_string(g.ERR_ALIGNMENT) == b"misaligned pointer or stride"
 
 
+def test_both_codecs_argument_checks(built):
+    """The two-codec pass checks what each single-codec call checks, plus its
+    second output; the single-output calls refuse the two-codec id."""
+    out, out2 = np.zeros(4096, np.uint8), np.zeros(4096, np.uint8)
+    img = np.zeros((64, 256), np.uint8)
+    assert g.compress_both_device(16, 24, 16, 6, 8, 64) == g.ERR_WIDTH
+    assert g.compress_both_device(16, 24, 16, 8, 6, 64) == g.ERR_HEIGHT
+    assert g.compress_both_device(16, None, 16, 8, 8, 64) == g.ERR_INVALID
+    assert g.compress_both_device(None, 24, 16, 8, 8, 64) == g.ERR_INVALID
+    assert g.compress_both_device(16, 24, 16, 8, 8, 16) == g.ERR_INVALID   # stride < 4*width
+    assert g.compress_both_device(16, 12, 16, 8, 8, 64) == g.ERR_ALIGNMENT  # ETC1s output not 8-byte aligned
+    assert g.compress_both_device(16, 24, 18, 8, 8, 64) == g.ERR_ALIGNMENT  # src not 4-byte aligned
+    assert g.compress_both_device(16, 24, 16, 0, 8, 64) == g.OK  # empty image: nothing to do
+    assert g.compress_both_host(out, None, img, 64, 64, 256) == g.ERR_INVALID
+    assert g.compress_both_host(out, out2, img, 62, 64, 256) == g.ERR_WIDTH
+    assert g.compress_device(g.CODEC_BOTH, 16, 16, 8, 8, 64) == g.ERR_INVALID
+    assert g.compress_host(g.CODEC_BOTH, out, img, 64, 64, 256) == g.ERR_INVALID
+
+
 def test_tile_get_set(built):
     for codec in (0, 1):
         before = g.get_tile(codec)
@@ -79,3 +98,9 @@ def test_tile_get_set(built):
         assert g.set_tile(codec, 96, 2) == g.ERR_INVALID
         assert g.set_tile(codec, 256, 3) == g.ERR_INVALID
         assert g.set_tile(codec, *before) == g.OK
+    # the two-codec pass has its own tile: 1 or 2 blocks a thread
+    before = g.get_tile(g.CODEC_BOTH)
+    assert g.set_tile(g.CODEC_BOTH, 256, 1, 2) == g.OK and g.get_tile(g.CODEC_BOTH) == (256, 1, 2)
+    assert g.set_tile(g.CODEC_BOTH, 256, 4, 0) == g.ERR_INVALID
+    assert g.set_tile(g.CODEC_BOTH, *before) == g.OK
+    assert g.set_tile(3, 256, 2, 0) == g.ERR_INVALID
