@@ -140,6 +140,7 @@ def _declare(lib):
         "goofy_gpu_psnr_rgb": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32,
                                               ctypes.POINTER(ctypes.c_double), _VP]),
         "goofy_gpu_pipeline_timeouts": (ctypes.c_int, [ctypes.POINTER(_U32), ctypes.c_int]),
+        "goofy_gpu_selftest_bounded_wait": (ctypes.c_int, [ctypes.POINTER(_U32)]),
         "goofy_gpu_mse_psnr": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, ctypes.POINTER(Quality)]),
         "goofy_gpu_png_info": (ctypes.c_int, [_VP, ctypes.c_size_t, ctypes.POINTER(_U32), ctypes.POINTER(_U32)]),
         "goofy_gpu_png_decode": (ctypes.c_int, [_VP, ctypes.c_size_t, _VP, ctypes.c_size_t, _U32, ctypes.c_int,
@@ -309,6 +310,14 @@ def pipeline_timeouts(reset=False):
     if rc != OK:
         raise RuntimeError("pipeline_timeouts: %s %s" % (status_string(rc), last_error()))
     return n.value
+
+
+def selftest_bounded_wait():
+    """(status, elapsed ms) of goofy_gpu_selftest_bounded_wait: a pipeline wait
+    on a barrier nothing completes gives up after its limit and is counted."""
+    ms = _U32()
+    rc = lib().goofy_gpu_selftest_bounded_wait(ctypes.byref(ms))
+    return rc, ms.value
 
 
 def autotune(codec, dst, src, width, height, stride, reps=9):

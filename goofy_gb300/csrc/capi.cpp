@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -531,6 +532,24 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
         best->persistent = best_tile.persistent;
     }
     if (best_us) *best_us = best_time * 1e3f;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_selftest_bounded_wait(uint32_t* elapsed_ms)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    bool completed = true, aborted = false;
+    unsigned int counted = 0;
+    CUDA_TRY(goofy_gpu::bounded_wait_selftest(&completed, &aborted, &counted));
+    if (elapsed_ms)
+        *elapsed_ms = (uint32_t)std::chrono::duration_cast<std::chrono::milliseconds>(
+                          std::chrono::steady_clock::now() - t0).count();
+    if (completed || !aborted || counted != 1) {
+        char what[128];
+        std::snprintf(what, sizeof what, "bounded wait self-test: completed %d, abort flag %d, time-outs counted %u",
+                      (int)completed, (int)aborted, counted);
+        return goofy_gpu::fail(GOOFY_ERR_CUDA, what);
+    }
     return GOOFY_OK;
 }
 

@@ -509,6 +509,41 @@ cudaError_t launch_batch_tma(const BatchImage* images, uint32_t n_images, const 
     return cudaErrorInvalidValue;
 }
 
+// Thread 0 waits on an mbarrier that expects one arrival and gets none.
+// Nothing is copied into the CTA, so nothing is in flight when it returns.
+__global__ void bounded_wait_selftest_kernel(unsigned int* counter, uint32_t* out)
+{
+    __shared__ uint64_t bar;
+    __shared__ uint32_t abort_flag;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1u);
+    abort_flag = 0u;
+    mbar_init_fence();
+    const bool completed = mbar_wait(&bar, 0u, &abort_flag, counter);
+    out[0] = completed ? 1u : 0u;
+    out[1] = abort_flag;
+}
+
+cudaError_t bounded_wait_selftest(bool* completed, bool* aborted, unsigned int* counted)
+{
+    uint32_t* d = nullptr;  // {counter, wait result, abort flag}
+    cudaError_t e = cudaMalloc(&d, 3 * sizeof(uint32_t));
+    if (e != cudaSuccess) return e;
+    uint32_t h[3] = {0, 0, 0};
+    e = cudaMemset(d, 0, 3 * sizeof(uint32_t));
+    if (e == cudaSuccess) {
+        bounded_wait_selftest_kernel<<<1, 32>>>(d, d + 1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    *counted = h[0];
+    *completed = h[1] != 0;
+    *aborted = h[2] != 0;
+    return e;
+}
+
 cudaError_t pipeline_timeouts(unsigned int* count, bool reset)
 {
     cudaError_t e = cudaMemcpyFromSymbol(count, g_pipeline_timeouts, sizeof(unsigned int));

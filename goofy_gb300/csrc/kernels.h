@@ -44,4 +44,9 @@ cudaError_t launch_image_tma(int codec, const uint8_t* src, size_t stride, uint8
 // Pipeline waits that gave up on the current device since the last reset.
 cudaError_t pipeline_timeouts(unsigned int* count, bool reset);
 
+// One bounded wait on a barrier that nothing completes (async_copy.cuh):
+// returns the wait's result (false: it gave up), whether it raised the abort
+// flag and how many time-outs it counted.  Synchronous.
+cudaError_t bounded_wait_selftest(bool* completed, bool* aborted, unsigned int* counted);
+
 }  // namespace goofy_gpu

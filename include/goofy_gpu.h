@@ -157,6 +157,15 @@ int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, ui
  * hanging); `reset` != 0 zeroes the count.  0 in a healthy run.  Synchronous. */
 int goofy_gpu_pipeline_timeouts(uint32_t* count, int reset);
 
+/* Self-test of the bounded waits on the current device.  One thread of a
+ * one-warp kernel waits on an mbarrier that nothing completes (no copy, no
+ * arrival); its wait gives up after the limit every pipeline wait has (1 s),
+ * raises its CTA's abort flag and counts one time-out in a counter of this
+ * call's own.  GOOFY_OK when exactly that happened and the kernel returned
+ * (the context stays usable), GOOFY_ERR_CUDA otherwise.  `elapsed_ms`, if not
+ * NULL, receives the call's wall time.  Synchronous, about one second. */
+int goofy_gpu_selftest_bounded_wait(uint32_t* elapsed_ms);
+
 /* ---- decoding and encode quality -------------------------------------------- */
 
 /* Decode (width/4)*(height/4) blocks (device) into RGBA8 rows (device,

@@ -251,3 +251,19 @@ def test_pipeline_reports_no_timeouts(cuda):
             np.testing.assert_array_equal(device_encode(cuda, codec, img, 1024, 512, tile=tile),
                                           oracle.encode(codec, img, 1024, 512))
     assert g.pipeline_timeouts() == 0
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable(cuda, golden):
+    """A pipeline wait on a barrier that nothing completes (no copy, no
+    arrival) gives up after its one-second limit, raises the abort flag and
+    counts once; the kernel returns and the next launches are bit-exact."""
+    before = g.pipeline_timeouts()
+    rc, ms = g.selftest_bounded_wait()
+    assert rc == g.OK, g.last_error()
+    assert 900 <= ms <= 10000, ms
+    assert g.pipeline_timeouts() == before  # the self-test counts in its own counter
+    w, h = int(golden["kat_width"]), int(golden["kat_height"])
+    for name, codec in CODECS:
+        for tile in ((512, 2, 2), (128, 2, 0)):
+            np.testing.assert_array_equal(device_encode(cuda, codec, golden["kat_input"], w, h, tile=tile),
+                                          golden["kat_" + name])
