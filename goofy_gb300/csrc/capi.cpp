@@ -193,6 +193,14 @@ int check_args(int codec, const void* dst, const void* src, uint32_t width, uint
     return 1;  // proceed
 }
 
+// The two outputs of the two-codec pass, (w/4)(h/4)*8 bytes each, must not overlap.
+bool outputs_overlap(const void* a, const void* b, uint32_t width, uint32_t height)
+{
+    const uint64_t n = (uint64_t)(width / 4) * (height / 4) * 8;
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + n && y < x + n;
+}
+
 constexpr size_t kBandBytes = 16u << 20;  // source bytes per band of the host path
 
 // Either codec into `dst`, or (codec GOOFY_CODEC_BOTH) the BC1 blocks into
@@ -203,7 +211,7 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
     const bool both = codec == GOOFY_CODEC_BOTH;
     int rc = check_args(both ? GOOFY_CODEC_BC1 : codec, dst, src, width, height, stride);
     if (rc <= 0) return rc;
-    if (both && !dst2) return GOOFY_ERR_INVALID;
+    if (both && (!dst2 || outputs_overlap(dst, dst2, width, height))) return GOOFY_ERR_INVALID;
     HostPath& hp = host_path();
     std::lock_guard<std::mutex> lk(hp.mu);
     if (!hp.ready) {
@@ -319,7 +327,7 @@ int compress_both_device_impl(void* dst_bc1, void* dst_etc1s, const void* src, u
 {
     int rc = check_args(GOOFY_CODEC_BC1, dst_bc1, src, width, height, stride);
     if (rc <= 0) return rc;
-    if (!dst_etc1s) return GOOFY_ERR_INVALID;
+    if (!dst_etc1s || outputs_overlap(dst_bc1, dst_etc1s, width, height)) return GOOFY_ERR_INVALID;
     if (reinterpret_cast<uintptr_t>(dst_bc1) % 8 != 0 || reinterpret_cast<uintptr_t>(dst_etc1s) % 8 != 0)
         return GOOFY_ERR_ALIGNMENT;
     const uintptr_t s = reinterpret_cast<uintptr_t>(src);

@@ -102,8 +102,8 @@ int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_
  * either way) and the per-block work both encoders share (channel extents, brightness range,
  * per-pixel luma sums) is done once.  No reference counterpart: the reference
  * harness calls the two encoders one after the other on every image
- * (Src/main.cpp:925-929).  Same rules as the single-codec calls; the two
- * outputs must not overlap.  Device form: async on `stream`, with the tile of
+ * (Src/main.cpp:925-929).  Same rules as the single-codec calls; outputs
+ * that overlap are refused (GOOFY_ERR_INVALID).  Device form: async on `stream`, with the tile of
  * GOOFY_CODEC_BOTH.  Host form: synchronous, pinned or pageable buffers. */
 int goofy_gpu_compress_both_device(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width,
                                    uint32_t height, uint32_t stride, void* stream);

@@ -71,14 +71,17 @@ def test_both_codecs_argument_checks(built):
     second output; the single-output calls refuse the two-codec id."""
     out, out2 = np.zeros(4096, np.uint8), np.zeros(4096, np.uint8)
     img = np.zeros((64, 256), np.uint8)
-    assert g.compress_both_device(16, 24, 16, 6, 8, 64) == g.ERR_WIDTH
-    assert g.compress_both_device(16, 24, 16, 8, 6, 64) == g.ERR_HEIGHT
+    assert g.compress_both_device(16, 4096, 16, 6, 8, 64) == g.ERR_WIDTH
+    assert g.compress_both_device(16, 4096, 16, 8, 6, 64) == g.ERR_HEIGHT
     assert g.compress_both_device(16, None, 16, 8, 8, 64) == g.ERR_INVALID
-    assert g.compress_both_device(None, 24, 16, 8, 8, 64) == g.ERR_INVALID
-    assert g.compress_both_device(16, 24, 16, 8, 8, 16) == g.ERR_INVALID   # stride < 4*width
-    assert g.compress_both_device(16, 12, 16, 8, 8, 64) == g.ERR_ALIGNMENT  # ETC1s output not 8-byte aligned
-    assert g.compress_both_device(16, 24, 18, 8, 8, 64) == g.ERR_ALIGNMENT  # src not 4-byte aligned
+    assert g.compress_both_device(None, 4096, 16, 8, 8, 64) == g.ERR_INVALID
+    assert g.compress_both_device(16, 4096, 16, 8, 8, 16) == g.ERR_INVALID   # stride < 4*width
+    assert g.compress_both_device(16, 4100, 16, 8, 8, 64) == g.ERR_ALIGNMENT  # ETC1s output not 8-byte aligned
+    assert g.compress_both_device(16, 4096, 18, 8, 8, 64) == g.ERR_ALIGNMENT  # src not 4-byte aligned
     assert g.compress_both_device(16, 24, 16, 0, 8, 64) == g.OK  # empty image: nothing to do
+    assert g.compress_both_device(4096, 4096 + 24, 16, 8, 8, 64) == g.ERR_INVALID  # outputs of 32 B overlap
+    assert g.compress_both_device(4096 + 24, 4096, 16, 8, 8, 64) == g.ERR_INVALID
+    assert g.compress_both_host(out, out[8:], img, 64, 64, 256) == g.ERR_INVALID
     assert g.compress_both_host(out, None, img, 64, 64, 256) == g.ERR_INVALID
     assert g.compress_both_host(out, out2, img, 62, 64, 256) == g.ERR_WIDTH
     assert g.compress_device(g.CODEC_BOTH, 16, 16, 8, 8, 64) == g.ERR_INVALID
