@@ -13,10 +13,11 @@
       images (decoded on the GPU) and the original and baseline images as
       TGA.
 
-  python -m goofy_gb300.tool encode IN.png OUT.dds|OUT.ktx [--codec bc1|etc1s] [--mips]
+  python -m goofy_gb300.tool encode IN.png OUT.dds|OUT.ktx [--codec bc1|etc1s] [--mips] [--both]
       One PNG to a DDS (BC1) or KTX (ETC1s) file, optionally with a full mip
       chain generated on the GPU (power-of-two sizes) and all levels encoded
-      in one batch launch.
+      in one batch launch.  --both writes OUT with the .dds and with the .ktx
+      extension from one pass per level (goofy_gpu_compress_both_device).
 """
 import argparse
 import ctypes
@@ -171,6 +172,8 @@ def cmd_encode(args):
         arena = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
         base = arena.data_ptr() + (-arena.data_ptr()) % 256
         levels = g.generate_mips(d_src, w, h, 4 * w, base, nbytes, stream)
+    if args.both:
+        return _encode_both(args, levels, stream, torch)
     outs = [torch.empty(g.out_size(lw, lh), dtype=torch.uint8, device="cuda") for _, lw, lh, _ in levels]
     batch = g.Batch(len(levels))
     try:
@@ -188,6 +191,29 @@ def cmd_encode(args):
     return 0
 
 
+def _encode_both(args, levels, stream, torch):
+    """Every level through the two-codec pass: the BC1 blocks to OUT.dds and
+    the ETC1s blocks to OUT.ktx, each level read once."""
+    outs = []
+    for p, lw, lh, s in levels:
+        n = g.out_size(lw, lh)
+        o = torch.empty(2 * n, dtype=torch.uint8, device="cuda")
+        rc = g.compress_both_device(o.data_ptr(), o.data_ptr() + n, p, lw, lh, s, stream)
+        if rc != g.OK:
+            raise SystemExit("encode failed: %s %s" % (g.status_string(rc), g.last_error()))
+        outs.append((o, n, lw, lh))
+    torch.cuda.synchronize()
+    stem = os.path.splitext(args.output)[0]
+    for codec, ext, half in ((g.CODEC_BC1, ".dds", 0), (g.CODEC_ETC1S, ".ktx", 1)):
+        host = [(o[half * n:(half + 1) * n].cpu().numpy(), lw, lh) for o, n, lw, lh in outs]
+        data = g.container(codec, host)
+        with open(stem + ext, "wb") as f:
+            f.write(data)
+        print("%s: %d level(s), %s, %d bytes" % (stem + ext, len(outs), "bc1" if codec == g.CODEC_BC1 else "etc1s",
+                                                len(data)))
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m goofy_gb300.tool", description=__doc__.split("\n")[0])
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -201,6 +227,7 @@ def main(argv=None):
     e.add_argument("output")
     e.add_argument("--codec", choices=("bc1", "etc1s"))
     e.add_argument("--mips", action="store_true", help="add a GPU-generated mip chain")
+    e.add_argument("--both", action="store_true", help="write OUT.dds and OUT.ktx from one pass over each level")
     args = ap.parse_args(argv)
     return cmd_run(args) if args.cmd == "run" else cmd_encode(args)
 

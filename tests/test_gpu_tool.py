@@ -39,6 +39,23 @@ def test_encode_with_mips(cuda, tmp_path, codec, ext):
     assert out.read_bytes() == want
 
 
+@pytest.mark.parametrize("mips", [False, True])
+def test_encode_both_formats_in_one_pass(cuda, tmp_path, mips):
+    """--both writes the DDS and the KTX file from one pass per level; each
+    equals the single-format file the oracle's blocks make."""
+    w, h = 128, 32
+    path, rgba = _png(tmp_path, "tex", w, h, 6)
+    argv = ["encode", str(path), str(tmp_path / "tex.dds"), "--both"] + (["--mips"] if mips else [])
+    assert tool.main(argv) == 0
+    chain, cur, cw, ch = [(rgba, w, h)], rgba, w, h
+    for _ in (workloads.mip_chain(w, h)[1:] if mips else []):
+        cur, cw, ch = workloads.downsample(cur, cw, ch)
+        chain.append((cur, cw, ch))
+    for c, ext in ((0, "dds"), (1, "ktx")):
+        want = g.container(c, [(oracle.encode(c, im, lw, lh), lw, lh) for im, lw, lh in chain])
+        assert (tmp_path / ("tex." + ext)).read_bytes() == want
+
+
 def test_run_prints_harness_rows(cuda, tmp_path):
     _png(tmp_path, "a", 64, 32, 1)
     _png(tmp_path, "b", 40, 32, 2)  # width % 16 != 0: refused as the harness refuses it
