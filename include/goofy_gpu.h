@@ -72,7 +72,7 @@ int goofy_gpu_compress_bc1_device(void* dst, const void* src, uint32_t width, ui
 int goofy_gpu_compress_etc1s_device(void* dst, const void* src, uint32_t width, uint32_t height,
                                     uint32_t stride, void* stream);
 
-/* Either codec (GOOFY_CODEC_*). */
+/* Either codec (GOOFY_CODEC_BC1 or GOOFY_CODEC_ETC1S). */
 int goofy_gpu_compress_device(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
                               uint32_t stride, void* stream);
 
@@ -90,6 +90,7 @@ int goofy_gpu_compress_bc1_host(uint8_t* dst, const uint8_t* src, uint32_t width
 int goofy_gpu_compress_etc1s_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                                   uint32_t stride);
 
+/* Either codec (GOOFY_CODEC_BC1 or GOOFY_CODEC_ETC1S). */
 int goofy_gpu_compress_host(int codec, uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                             uint32_t stride);
 
