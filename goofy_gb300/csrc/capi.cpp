@@ -2,8 +2,11 @@
 //
 // Reference interface replaced: goofy::compressDXT1 / goofy::compressETC1
 // (GoofyTC/goofy_tc.h:10-13, :1497-1557), a synchronous CPU function over
-// caller-owned host buffers.  Here the same call streams the image through
-// the GPU: the rows are split into bands, and for each band
+// caller-owned host buffers.  Here the same call runs on the GPU.  Direct
+// path: when the GPU can address both buffers (pinned, or any host memory
+// where it walks the host page tables), one kernel reads the caller's rows
+// and writes its blocks over the host link.  Staged path: the rows are split
+// into bands, and for each band
 //   host -> device copy, encode kernel, device -> host copy
 // are queued on one of two streams, so the copy-in of band b+1 overlaps the
 // encode and copy-out of band b.  Pinned caller buffers are copied by DMA

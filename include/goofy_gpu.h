@@ -80,9 +80,13 @@ int goofy_gpu_compress_device(int codec, void* dst, const void* src, uint32_t wi
 
 /* Host-memory counterpart of goofy::compressDXT1 (goofy_tc.h:1497-1526): same
  * arguments and output, returns when `dst` holds the result.  Pinned or
- * pageable buffers of any alignment; width % 4 == 0, height % 4 == 0.  The
- * image is streamed through the GPU in bands (copy in / encode / copy out
- * overlapped on two streams).  Thread-safe (calls are serialised). */
+ * pageable buffers of any alignment; width % 4 == 0, height % 4 == 0.  When
+ * the GPU can address both buffers (pinned memory, or any host memory where
+ * it walks the host page tables, as on Grace-Blackwell) and they are word
+ * aligned, one kernel reads the rows and writes the blocks over the host
+ * link; otherwise the image is streamed through device memory in bands (copy
+ * in / encode / copy out overlapped on two streams).  See
+ * goofy_gpu_set_host_path.  Thread-safe (calls are serialised). */
 int goofy_gpu_compress_bc1_host(uint8_t* dst, const uint8_t* src, uint32_t width, uint32_t height,
                                 uint32_t stride);
 
