@@ -21,6 +21,8 @@ previous launch did not touch (inputs larger than the 129 MB L2).
 * cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
 * both_codecs_one_pass -- beside the headline: the same two outputs from one
                 read of the image (goofy_gpu_compress_both_*), device and host.
+* cold_configs -- the 256x256 scene and the 4096x4096 stress image, each
+                launch timed alone with L2 flushed before it.
 
 ``--impl reference`` times the reference's CPU implementation of the path on
 this host's cores instead (the reference compiled from its own sources where
@@ -273,6 +275,45 @@ def run_dropin_latency(g, img, sides=(256, 1024, 4096), calls=50):
     res["note"] = ("median wall time of one drop-in call from Python (ctypes) with pageable numpy buffers, "
                    "%d calls per entry; it includes a kernel launch and a stream synchronisation" % calls)
     return res
+
+
+def run_cold_configs(g, torch, workloads, codecs, stream, reps=20):
+    """The two other single-image workloads, timed cold: the 256x256 scene
+    (seed 0, launch-latency bound, L2-resident once warm) and the 4096x4096
+    stress quarters (seed 2).  Before each launch a 256 MiB buffer is written,
+    which leaves none of the image in the 129 MB L2; each launch is bracketed
+    by its own two CUDA events.  Median and min of `reps` launches."""
+    sh = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=stream.device)
+    cases = [("256x256 scene (seed 0, stride 1024 B)", 256, workloads.scene(256, 256, 0)),
+             ("4096x4096 stress quarters (seed 2: uniform noise, constant blocks, two-colour blocks, grey with "
+              "random alpha)", 4096, workloads.stress(4096, 4096, 2))]
+    out = {}
+    for name, side, img in cases:
+        src = torch.from_numpy(img.reshape(-1)).to(stream.device)
+        dst = torch.empty(g.out_size(side, side), dtype=torch.uint8, device=stream.device)
+        row = {"workload": name}
+        for c in codecs:
+            ts = []
+            for r in range(reps + 2):
+                flush.fill_(r & 0xff)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rc = g.compress_device(c, dst.data_ptr(), src.data_ptr(), side, side, 4 * side, sh)
+                e1.record(stream)
+                if rc != g.OK:
+                    raise RuntimeError("%s: %s" % (name, g.last_error()))
+                e1.synchronize()
+                if r >= 2:
+                    ts.append(e0.elapsed_time(e1) * 1e3)
+            med = statistics.median(ts)
+            row["bc1" if c == g.CODEC_BC1 else "etc1s"] = {
+                "median_us": round(med, 2), "min_us": round(min(ts), 2),
+                "mpix_s": round(side * side / med, 1), "hbm_gbs": round(ALG_BYTES_PER_PX * side * side / med / 1e3, 1)}
+        out["%dx%d" % (side, side)] = row
+    out["timing"] = ("each launch between its own two CUDA events after a 256 MiB write (L2 cold), %d launches "
+                     "after 2 untimed ones, default tiles" % reps)
+    return out
 
 
 def run_pair(args, g, torch, src, dst, codecs, stream, device):
@@ -909,6 +950,7 @@ def run_gpu(args):
     pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
     two_streams = run_two_streams(args, g, torch, src, dst, codecs, stream) if single else None
     both = run_both(args, g, torch, img, src, dst, codecs, stream) if single else None
+    cold = run_cold_configs(g, torch, workloads, codecs, stream) if single else None
     batched = None
     if not args.no_batched and single:
         batched = run_batched(args, g, torch, stream, dev)
@@ -927,7 +969,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "both_codecs_one_pass": both, "batched": batched,
+            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "both_codecs_one_pass": both, "cold_configs": cold, "batched": batched,
             "serving": serving,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
