@@ -363,6 +363,10 @@ def run_both(args, g, torch, img, src, dst, codecs, stream):
     sh = stream.cuda_stream
     n = g.out_size(W, H)
     outs = [torch.empty(2 * n, dtype=torch.uint8, device=src[0].device) for _ in range(2)]
+    tuned = None
+    if not args.no_autotune:
+        tile, us = g.autotune(g.CODEC_BOTH, outs[0].data_ptr(), src[0].data_ptr(), W, H, 4 * W, reps=7)
+        tuned = {"tile": list(tile), "median_us": round(us, 2)}
 
     def launch(k):
         o = outs[k % 2].data_ptr()
@@ -383,7 +387,7 @@ def run_both(args, g, torch, img, src, dst, codecs, stream):
     exact = all(bool(torch.equal(outs[k][:n], dst[codecs[0]]) and torch.equal(outs[k][n:], dst[codecs[1]]))
                 for k in range(2))
     res = {"api": "goofy_gpu_compress_both_device: BC1 + ETC1s blocks of one image from one read of it",
-           "tile": list(g.get_tile(g.CODEC_BOTH)), "mean_launch_us": round(1e3 * ms, 2),
+           "tile": list(g.get_tile(g.CODEC_BOTH)), "autotune": tuned, "mean_launch_us": round(1e3 * ms, 2),
            "image_mpix_s": round(W * H / (ms / 1e3) / 1e6, 1),
            "codec_mpix_s": round(2 * W * H / (ms / 1e3) / 1e6, 1),
            "hbm_gbs": round(5.0 * W * H / (ms / 1e3) / 1e9, 1), "algorithmic_bytes_per_px": 5.0,

@@ -478,7 +478,8 @@ GOOFY_EXPORT int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile)
 GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
                                    uint32_t stride, uint32_t reps, goofy_gpu_tile* best, float* best_us)
 {
-    int rc = check_args(codec, dst, src, width, height, stride);
+    const bool both = codec == GOOFY_CODEC_BOTH;  // dst: the BC1 blocks, then the ETC1s blocks
+    int rc = check_args(both ? GOOFY_CODEC_BC1 : codec, dst, src, width, height, stride);
     if (rc <= 0) return rc == GOOFY_OK ? GOOFY_ERR_INVALID : rc;
     if (reps == 0 || reps > 1000) return GOOFY_ERR_INVALID;
     const uintptr_t s = reinterpret_cast<uintptr_t>(src);
@@ -497,13 +498,14 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
     for (uint32_t persistent : {0u, 1u, 2u})
         for (uint32_t threads : {128u, 256u, 512u})
             for (uint32_t bpt : {1u, 2u, 4u})
-                if (goofy_gpu::tile_valid(Tile{threads, bpt, persistent}))
+                if (goofy_gpu::tile_valid(Tile{threads, bpt, persistent}) && !(both && (bpt > 2 || persistent == 1)))
                     candidates.push_back(Tile{threads, bpt, persistent});
+    uint8_t* const dst2 = both ? static_cast<uint8_t*>(dst) + (size_t)(width / 4) * (height / 4) * 8 : nullptr;
     for (const Tile& t : candidates) {
         if (result != GOOFY_OK) break;
         auto launch = [&] {
             return goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
-                                           width, height, t, access, st);
+                                           width, height, t, access, st, dst2);
         };
         // three rounds of `reps` launches back to back between two events (an
         // event between two launches would delay the second one's start); the

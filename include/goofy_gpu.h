@@ -153,7 +153,9 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
  * events -- after two warm-up launches, three rounds of `reps` launches back to
  * back between two events, the median round's mean kept -- installs the
  * fastest as the codec's tile and returns it with that mean launch time in
- * microseconds.  Synchronous.  No reference counterpart. */
+ * microseconds.  Synchronous.  No reference counterpart.  GOOFY_CODEC_BOTH
+ * tunes the two-codec pass: `dst` then holds both outputs back to back
+ * (2 * (width/4)(height/4)*8 bytes, the BC1 blocks first). */
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
 

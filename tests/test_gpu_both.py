@@ -146,3 +146,26 @@ def test_full_size_scene_8192(cuda):
     finally:
         g.set_tile(g.CODEC_BOTH, *before)
     assert g.pipeline_timeouts() == 0
+
+
+def test_autotune_the_two_codec_pass(cuda):
+    """GOOFY_CODEC_BOTH autotunes the two-codec pass over a buffer holding
+    both outputs; the installed tile is one the pass runs, and its outputs
+    stay bit-exact."""
+    w = h = 1024
+    img = workloads.scene(w, h, 17, period_scale=4, rects=64)
+    n = g.out_size(w, h)
+    src = cuda.from_numpy(img.reshape(-1)).cuda()
+    out = cuda.zeros(2 * n, dtype=cuda.uint8, device="cuda")
+    before = g.get_tile(g.CODEC_BOTH)
+    try:
+        tile, us = g.autotune(g.CODEC_BOTH, out, src, w, h, 4 * w, reps=3)
+        assert g.get_tile(g.CODEC_BOTH) == tile and tile[1] <= 2 and tile[2] != 1 and us > 0
+        assert g.compress_both_device(out, out.data_ptr() + n, src, w, h, 4 * w,
+                                      cuda.cuda.current_stream().cuda_stream) == g.OK
+        cuda.cuda.synchronize()
+        got = out.cpu().numpy()
+        np.testing.assert_array_equal(got[:n], oracle.encode(0, img, w, h))
+        np.testing.assert_array_equal(got[n:], oracle.encode(1, img, w, h))
+    finally:
+        g.set_tile(g.CODEC_BOTH, *before)
