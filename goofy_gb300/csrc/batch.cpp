@@ -8,7 +8,9 @@
 // batch are written while the previous batch still runs; a slot is refilled
 // only after the launch that used it completed.  Each encode is one H2D copy
 // (descriptors, first-unit table and a zeroed work counter, one buffer) and
-// the persistent kernel, enqueued on the caller's stream.  With graphs enabled
+// the persistent kernel, enqueued on the caller's stream (a pipelined batch
+// of at most kInlineImages images instead passes its descriptors as the
+// kernel's parameter: one launch, no upload).  With graphs enabled
 // the two are captured once per slot (on the library's own idle stream) and
 // the graph is launched on the caller's stream while the batch shape (image
 // count, work units, tile) stays the same; the pointers inside the
@@ -129,6 +131,19 @@ int encode_locked(goofy_gpu_batch* b, const goofy_gpu_image* images, uint32_t co
     if (count == 0) return GOOFY_OK;
     DeviceGuard g(b->device);
     GOOFY_CUDA_TRY(g.err);
+    if (tile.pipeline && count <= goofy_gpu::kInlineImages) {
+        // a small pipelined batch: its descriptors travel as the kernel's parameter (no upload, no graph)
+        goofy_gpu::InlineBatch ib{};
+        uint32_t units = 0;
+        const int rc = validate_and_fill(images, count, tile.unit_blocks, ib.images, ib.first_unit, &units);
+        if (rc != GOOFY_OK) return rc;
+        if (units == 0) return GOOFY_OK;
+        const uint32_t ctas = (uint32_t)std::min<uint64_t>(
+            (uint64_t)goofy_gpu::batch_resident_ctas(tile.threads, tile.bpt, tile.pipeline), units);
+        const cudaError_t e = goofy_gpu::launch_batch_tma_inline(ib, count, units, tile, ctas, caller);
+        if (e != cudaSuccess) return cuda_fail(e, "batch launch");
+        return GOOFY_OK;
+    }
     Slot& s = b->slot[b->next];
     b->next ^= 1;
     if (s.in_flight) {

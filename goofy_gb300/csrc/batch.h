@@ -49,6 +49,16 @@ cudaError_t launch_batch_tma(const BatchImage* images, uint32_t n_images, const 
                              uint32_t total_units, uint32_t* work_counter, const BatchTile& tile, uint32_t ctas,
                              cudaStream_t stream);
 
+// A pipelined batch of at most kInlineImages images, passed by value as the
+// kernel's parameter (3.3 KB): the launch needs no descriptor upload.
+constexpr uint32_t kInlineImages = 64;
+struct InlineBatch {
+    BatchImage images[kInlineImages];
+    uint32_t first_unit[kInlineImages];
+};
+cudaError_t launch_batch_tma_inline(const InlineBatch& batch, uint32_t n_images, uint32_t total_units,
+                                    const BatchTile& tile, uint32_t ctas, cudaStream_t stream);
+
 // Enqueue the persistent batch kernel.  `work_counter` must read 0 when the
 // kernel starts; `first_unit[i]` is images[i].first_unit (ascending, [0] = 0).
 cudaError_t launch_batch(const BatchImage* images, uint32_t n_images, const uint32_t* first_unit,

@@ -213,9 +213,8 @@ constexpr size_t batch_tma_smem_bytes(const TmaLayout& l)
 }
 
 template <int BPT, int COMPUTE>
-__global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
-    encode_batch_tma(const BatchImage* __restrict__ images, uint32_t n_images, const uint32_t* __restrict__ first_unit,
-                     uint32_t total_units)
+__device__ __forceinline__ void batch_tma_body(const BatchImage* __restrict__ images, uint32_t n_images,
+                                               const uint32_t* __restrict__ first_unit, uint32_t total_units)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t abort_flag;
@@ -360,6 +359,23 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     }
 }
 
+// Descriptor and first-unit tables in device memory (uploaded per call).
+template <int BPT, int COMPUTE>
+__global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
+    encode_batch_tma(const BatchImage* __restrict__ images, uint32_t n_images, const uint32_t* __restrict__ first_unit,
+                     uint32_t total_units)
+{
+    batch_tma_body<BPT, COMPUTE>(images, n_images, first_unit, total_units);
+}
+
+// The same tables in the kernel's parameter space (small batches).
+template <int BPT, int COMPUTE>
+__global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
+    encode_batch_tma_inline(const __grid_constant__ InlineBatch batch, uint32_t n_images, uint32_t total_units)
+{
+    batch_tma_body<BPT, COMPUTE>(batch.images, n_images, batch.first_unit, total_units);
+}
+
 namespace {
 
 template <int CODEC, int BPT, int COMPUTE>
@@ -476,7 +492,51 @@ cudaError_t launch_batch_tma_t(const BatchImage* images, uint32_t n_images, cons
     return cudaGetLastError();
 }
 
+template <int BPT, int COMPUTE>
+cudaError_t launch_batch_tma_inline_t(const InlineBatch& batch, uint32_t n_images, uint32_t total_units, uint32_t ctas,
+                                      cudaStream_t stream)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int resident = batch_tma_ctas_t<BPT, COMPUTE>(dev);
+    if (resident == 0 || dev < 0 || dev >= 64) return cudaErrorInvalidValue;
+    constexpr size_t smem = batch_tma_smem_bytes(tma_layout(COMPUTE, BPT));
+    static std::atomic<bool> ready[64];
+    if (!ready[dev].load(std::memory_order_relaxed)) {
+        e = cudaFuncSetAttribute(encode_batch_tma_inline<BPT, COMPUTE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(encode_batch_tma_inline<BPT, COMPUTE>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        ready[dev].store(true, std::memory_order_relaxed);
+    }
+    if (ctas > (uint32_t)resident) ctas = (uint32_t)resident;
+    encode_batch_tma_inline<BPT, COMPUTE><<<ctas ? ctas : 1u, COMPUTE + 32, smem, stream>>>(batch, n_images,
+                                                                                             total_units);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_batch_tma_inline(const InlineBatch& batch, uint32_t n_images, uint32_t total_units,
+                                    const BatchTile& tile, uint32_t ctas, cudaStream_t stream)
+{
+    if (total_units == 0) return cudaSuccess;
+    if (n_images > kInlineImages || tile.unit_blocks != tile.threads * tile.bpt) return cudaErrorInvalidValue;
+    const uint32_t t = tile.threads;
+    if (tile.bpt == 1) {
+        if (t == 128) return launch_batch_tma_inline_t<1, 128>(batch, n_images, total_units, ctas, stream);
+        if (t == 256) return launch_batch_tma_inline_t<1, 256>(batch, n_images, total_units, ctas, stream);
+        if (t == 512) return launch_batch_tma_inline_t<1, 512>(batch, n_images, total_units, ctas, stream);
+    } else if (tile.bpt == 2) {
+        if (t == 128) return launch_batch_tma_inline_t<2, 128>(batch, n_images, total_units, ctas, stream);
+        if (t == 256) return launch_batch_tma_inline_t<2, 256>(batch, n_images, total_units, ctas, stream);
+        if (t == 512) return launch_batch_tma_inline_t<2, 512>(batch, n_images, total_units, ctas, stream);
+    }
+    return cudaErrorInvalidValue;
+}
 
 int batch_tma_resident_ctas(uint32_t threads, uint32_t bpt)
 {

@@ -311,9 +311,11 @@ void goofy_gpu_batch_destroy(goofy_gpu_batch* batch);
  * (runs of unit_blocks blocks of one image) from a device work counter, or
  * with a pipeline tile each CTA's producer warp stages its units' rows in
  * shared memory.  Enqueued on `stream` (one descriptor upload and the
- * kernel, a CUDA graph replay for a repeated batch shape): ordered after the
- * work already queued there, and later work there waits for it.  Each
- * image's output equals goofy_gpu_compress_device on that image alone. */
+ * kernel, a CUDA graph replay for a repeated batch shape; with a pipeline
+ * tile and at most 64 images, the descriptors are the kernel's parameter and
+ * nothing is uploaded): ordered after the work already queued there, and
+ * later work there waits for it.  Each image's output equals
+ * goofy_gpu_compress_device on that image alone. */
 int goofy_gpu_batch_encode(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, void* stream);
 
 /* CUDA-graph replay of same-shaped batches (default on). */

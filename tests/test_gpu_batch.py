@@ -129,6 +129,28 @@ def test_batch_tiles(cuda, mixed, tile):
         b.close()
 
 
+@pytest.mark.parametrize("count", [1, 2, 63, 64, 65])
+def test_pipelined_small_batches_pass_descriptors_inline(cuda, mixed, count):
+    """A pipelined batch of at most 64 images passes its descriptors as the
+    kernel's parameter instead of uploading them (65 takes the upload); both
+    give every image's own blocks, with graphs on and off."""
+    assert len(mixed) > 65
+    items = mixed[:count]
+    b = g.Batch(len(mixed))
+    try:
+        stream = cuda.cuda.current_stream().cuda_stream
+        for tile in ((512, 2, 1024, 1), (128, 1, 128, 1)):
+            assert b.set_tile(*tile) == g.OK
+            for graphs in (True, False):
+                b.set_graphs(graphs)
+                reset(items)
+                assert b.encode(descriptors(items), stream) == g.OK, g.last_error()
+                check(cuda, items)
+    finally:
+        b.close()
+    assert g.pipeline_timeouts() == 0
+
+
 def test_batch_autotune(cuda, mixed):
     b = g.Batch(len(mixed))
     try:
