@@ -84,3 +84,85 @@ def test_peak_is_the_measured_copy_bandwidth():
         assert kind == "measured" and peak == float(json.load(open(path))["hbm_gbs"])
     else:
         assert (peak, kind) == (6800.0, "fallback")
+
+
+class _FakeTensor:
+    def __init__(self, n):
+        self.n = n
+
+    def fill_(self, v):
+        return self
+
+    def to(self, device):
+        return self
+
+    def reshape(self, *a):
+        return self
+
+    def data_ptr(self):
+        return 4096
+
+
+class _FakeEvent:
+    clock = [0.0]
+
+    def __init__(self, enable_timing=False):
+        self.t = None
+
+    def record(self, stream):
+        _FakeEvent.clock[0] += 0.005  # 5 us between consecutive records
+        self.t = _FakeEvent.clock[0]
+
+    def synchronize(self):
+        pass
+
+    def elapsed_time(self, other):
+        return other.t - self.t
+
+
+class _FakeTorch:
+    uint8 = "u8"
+
+    class cuda:
+        Event = _FakeEvent
+
+    @staticmethod
+    def empty(n, dtype=None, device=None):
+        return _FakeTensor(n)
+
+    @staticmethod
+    def from_numpy(a):
+        return _FakeTensor(a.size)
+
+
+def test_cold_configs_bookkeeping():
+    """run_cold_configs: one flush and one bracketed launch per rep, two
+    untimed ones first, median / min / rates per codec and workload."""
+    import types
+
+    import numpy as np
+
+    calls = []
+
+    class FakeLib:
+        OK, CODEC_BC1, CODEC_ETC1S = 0, 0, 1
+
+        def out_size(self, w, h):
+            return w * h // 2
+
+        def compress_device(self, c, dst, src, w, h, stride, sh):
+            calls.append((c, w, h, stride))
+            return 0
+
+        def last_error(self):
+            return ""
+
+    work = types.SimpleNamespace(scene=lambda w, h, s: np.zeros((h, 4 * w), np.uint8),
+                                 stress=lambda w, h, s: np.zeros((h, 4 * w), np.uint8))
+    stream = types.SimpleNamespace(cuda_stream=0, device="cuda:0")
+    res = bench.run_cold_configs(FakeLib(), _FakeTorch, work, (0, 1), stream, reps=4)
+    assert set(res) == {"256x256", "4096x4096", "timing"}
+    assert len(calls) == 2 * 2 * (4 + 2) and {(w, s) for _, w, _, s in calls} == {(256, 1024), (4096, 16384)}
+    r = res["4096x4096"]["etc1s"]
+    assert r["median_us"] == r["min_us"] == 5.0  # every launch spans one 5 us tick of the fake clock
+    assert r["mpix_s"] == round(4096 * 4096 / 5.0, 1) and r["hbm_gbs"] == round(4.5 * 4096 * 4096 / 5.0 / 1e3, 1)
