@@ -68,6 +68,10 @@ def test_edge_blocks_vs_oracle(emu):
     img = np.ascontiguousarray(img)
     for codec in (0, 1):
         np.testing.assert_array_equal(_encode(emu, codec, img, w, h), oracle.encode(codec, img, w, h))
+    # the two-codec pass on the same blocks
+    bc1, etc = _encode_both(emu, img, w, h)
+    np.testing.assert_array_equal(bc1, oracle.encode(0, img, w, h))
+    np.testing.assert_array_equal(etc, oracle.encode(1, img, w, h))
 
 
 def _encode_both(emu, img, w, h):
