@@ -1,20 +1,24 @@
 """Oracle package -- TEST INFRASTRUCTURE ONLY.
 
 ``load()`` returns the ctypes handle of the C restatement (goofy_oracle.c);
-``load_ref()`` the reference encoder compiled from its own header (None where
-the reference tree is absent, e.g. on an aarch64 host).  Only tests/,
-__graft_entry__.smoke() and bench.py's CPU legs use these; the product
+``load_ref()`` the reference encoder compiled from its own header with its
+SSE2 path (None where the reference tree is absent or the host is not
+x86-64); ``load_ref_scalar()`` the reference encoder's own scalar path, built
+from the header copy without goofy_tc.h:16 (None where that copy was never
+generated); ``ref_encoder()`` the best of these for a CPU baseline.  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU legs use these; the product
 package never imports this module.
 """
 import ctypes
 import os
 
-from .build import ORACLE_SO, REF_SO
+from .build import ORACLE_SO, REF_SCALAR_SO, REF_SO
 
 _VP = ctypes.c_void_p
 _U = ctypes.c_uint
 _oracle = None
 _ref = None
+_ref_scalar = None
 
 
 def load():
@@ -42,6 +46,8 @@ def load():
         lib.oracle_mse_psnr.argtypes = [_VP, _U, _VP, _U, _U, _U, _VP]
         lib.oracle_psnr_rgb.restype = ctypes.c_double
         lib.oracle_psnr_rgb.argtypes = [_VP, _U, _U]
+        lib.goofy_synth_scene.restype = ctypes.c_int
+        lib.goofy_synth_scene.argtypes = [_VP, _U, _U, _U, ctypes.c_uint64, _U, _U, ctypes.c_int]
         _oracle = lib
     return _oracle
 
@@ -62,6 +68,46 @@ def load_ref():
                                        ctypes.POINTER(_U)]
         _ref = lib
     return _ref
+
+
+def load_ref_scalar():
+    """The reference encoder's scalar path (GOOFY_SSE2 undefined), else None."""
+    global _ref_scalar
+    if _ref_scalar is None and os.path.exists(REF_SCALAR_SO):
+        lib = ctypes.CDLL(REF_SCALAR_SO)
+        lib.ref_compress.restype = ctypes.c_int
+        lib.ref_compress.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U]
+        lib.ref_compress_mt.restype = ctypes.c_int
+        lib.ref_compress_mt.argtypes = [ctypes.c_int, _VP, _VP, _U, _U, _U, ctypes.c_int]
+        _ref_scalar = lib
+    return _ref_scalar
+
+
+def ref_encoder():
+    """(compress_mt function, kind, label) of the reference's own CPU encoder
+    for a baseline: its SSE2 path where built, else its scalar path, else the
+    oracle port (kind "port")."""
+    ref = load_ref()
+    if ref is not None:
+        return ref.ref_compress_mt, "reference", "reference goofy_tc.h, SSE2 path"
+    ref = load_ref_scalar()
+    if ref is not None:
+        return (ref.ref_compress_mt, "reference",
+                "reference goofy_tc.h, its portable scalar path (GOOFY_SSE2 undefined; SSE2 is x86-only)")
+    return load().oracle_compress_mt, "port", "oracle port of the reference encoder (reference not built here)"
+
+
+def scene(w, h, seed, period_scale=1, rects=8, threads=0):
+    """The synthetic scene (goofy_gb300/csrc/synth.c, compiled into the oracle
+    library) as an (h, 4w) RGBA8 array with 256-byte aligned rows."""
+    import numpy as np
+
+    raw = np.empty(h * 4 * w + 256, np.uint8)
+    off = (-raw.ctypes.data) % 256
+    img = raw[off:off + h * 4 * w].reshape(h, 4 * w)
+    if load().goofy_synth_scene(img.ctypes.data, w, h, 4 * w, seed, period_scale, rects, threads) != 0:
+        raise ValueError("goofy_synth_scene failed")
+    return img
 
 
 def encode(codec, img, width, height, stride=None, threads=1, any_width=True):

@@ -8,10 +8,15 @@
 // ships with; a debug build asserts 64-byte aligned strips (goofy_tc.h:1072).
 // goofy_tc.h defines its functions non-inline (goofy_tc.h:34), so it is
 // included in this one translation unit only.
+// Built a second time with GOOFY_REF_ENCODER_ONLY from the header copy that
+// oracle/build.py generates without goofy_tc.h:16 (the reference's scalar
+// path, for hosts without SSE2): the encoder entry points only.
 #include "goofy_tc.h"
 
+#ifndef GOOFY_REF_ENCODER_ONLY
 #include "decoder.h"
 #include "lodepng.h"
+#endif
 
 #include <thread>
 #include <vector>
@@ -48,6 +53,7 @@ extern "C" int ref_compress_mt(int codec, unsigned char* result, const unsigned 
     return threads;
 }
 
+#ifndef GOOFY_REF_ENCODER_ONLY
 // The reference harness's block decoders (Src/decoder.cpp:933-971): one
 // block into 16 RGBA8 pixels, 16-byte rows.
 extern "C" void ref_decode_block(int codec, const unsigned char* blk, unsigned char* out64)
@@ -69,3 +75,4 @@ extern "C" unsigned ref_png_decode(const unsigned char* png, size_t n, unsigned 
     std::copy(img.begin(), img.end(), out);
     return 0;
 }
+#endif  // GOOFY_REF_ENCODER_ONLY

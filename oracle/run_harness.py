@@ -14,9 +14,10 @@ import os
 import platform
 import subprocess
 
+from .build import REFERENCE
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 RUN_DIR = os.path.join(HERE, "_ref", "harness")
-REFERENCE = "/root/reference"
 BINARY = os.path.join(RUN_DIR, "goofy_harness")
 FIELDS = ("image", "encoder", "format", "pixels", "time_us", "mps", "mse_r", "mse_g", "mse_b", "mse_max", "mse_rgb",
           "mse_y", "psnr_r", "psnr_g", "psnr_b", "psnr_min", "psnr_rgb", "psnr_y", "delta_min", "delta_rgb",

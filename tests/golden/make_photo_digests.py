@@ -33,8 +33,8 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 from oracle import run_harness  # noqa: E402
+from oracle.build import TEST_DATA  # noqa: E402
 
-TEST_DATA = "/root/reference/test-data"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "photo_digests.json")
 CODECS = ("bc1", "etc1s")
 

@@ -10,9 +10,10 @@ import pytest
 
 import goofy_gb300 as g
 import oracle
+from oracle.build import TEST_DATA
 from goofy_gb300 import workloads
 
-PARROT = "/root/reference/test-data/parrot_red.png"
+PARROT = os.path.join(TEST_DATA, "parrot_red.png")
 # md5 of the reference harness's parrot_red_simd_goofy_dxt1.dds / _etc1.ktx
 REF_MD5 = {0: "72e3e448ff684294a9158859101645a3", 1: "affe18054aea11c5bdbe20841a414fbc"}
 

@@ -8,9 +8,10 @@ import numpy as np
 import pytest
 
 import oracle
+from oracle.build import TEST_DATA
 from goofy_gb300 import workloads
 
-PARROT = "/root/reference/test-data/parrot_red.png"
+PARROT = os.path.join(TEST_DATA, "parrot_red.png")
 
 
 def _ref():

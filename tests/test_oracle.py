@@ -114,3 +114,36 @@ def test_reference_error_codes(built):
     out = np.zeros(4096, np.uint8)
     assert ref.ref_compress(0, out.ctypes.data, img.ctypes.data, 60, 64, 256) == -1
     assert ref.ref_compress(1, out.ctypes.data, img.ctypes.data, 64, 62, 256) == -2
+
+
+def test_reference_scalar_path_matches_sse2_path_and_oracle(built):
+    """The reference's own scalar path (the generated header copy without
+    goofy_tc.h:16, the CPU baseline on hosts without SSE2) gives the blocks of
+    its SSE2 path and of the oracle, block for block, and keeps the error codes."""
+    scalar = oracle.load_ref_scalar()
+    if scalar is None:
+        pytest.skip("the scalar header copy was never generated on this host")
+    ref = oracle.load_ref()
+    rng = np.random.default_rng(9)
+    w, h = 512, 256
+    imgs = [_aligned(rng.integers(0, 256, (h, 4 * w)).astype(np.uint8)),
+            _aligned(workloads.scene(w, h, 4, rects=32)), _aligned(workloads.stress(w, h, 2))]
+    for img in imgs:
+        for codec in (0, 1):
+            got = np.zeros(w * h // 2, np.uint8)
+            assert scalar.ref_compress_mt(codec, got.ctypes.data, img.ctypes.data, w, h, 4 * w, 3) == 3
+            np.testing.assert_array_equal(got, oracle.encode(codec, img, w, h, any_width=False))
+            if ref is not None:
+                want = np.zeros_like(got)
+                assert ref.ref_compress(codec, want.ctypes.data, img.ctypes.data, w, h, 4 * w) == 0
+                np.testing.assert_array_equal(got, want)
+    out = np.zeros(4096, np.uint8)
+    assert scalar.ref_compress(0, out.ctypes.data, imgs[0].ctypes.data, 60, 64, 4 * w) == -1
+    assert scalar.ref_compress(1, out.ctypes.data, imgs[0].ctypes.data, 64, 62, 4 * w) == -2
+
+
+def test_oracle_scene_generator_is_the_libraries_generator(built):
+    """The CPU arm of the benchmark makes its scene with the generator compiled
+    into the oracle library; it equals the one the GPU arm uses."""
+    np.testing.assert_array_equal(oracle.scene(768, 256, 1, period_scale=3, rects=40),
+                                  workloads.scene(768, 256, 1, period_scale=3, rects=40))

@@ -12,9 +12,9 @@ import pytest
 
 import goofy_gb300 as g
 import oracle
+from oracle.build import TEST_DATA
 
 DIGESTS = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "photo_digests.json")))
-TEST_DATA = os.environ.get("GOOFY_TEST_DATA", "/root/reference/test-data")
 CODECS = {"DXT1": "bc1", "ETC1": "etc1s"}
 
 

@@ -12,9 +12,9 @@ import pytest
 
 import goofy_gb300 as g
 import oracle
+from oracle.build import TEST_DATA
 from tests.pngwrite import expected_rgba, write_png
 
-TEST_DATA = os.environ.get("GOOFY_TEST_DATA", "/root/reference/test-data")
 FORMATS = [(0, 1), (0, 2), (0, 4), (0, 8), (0, 16), (2, 8), (2, 16), (3, 1), (3, 2), (3, 4), (3, 8),
            (4, 8), (4, 16), (6, 8), (6, 16)]
 STRATEGIES = [(0, zlib.Z_DEFAULT_STRATEGY), (9, zlib.Z_DEFAULT_STRATEGY), (6, zlib.Z_FIXED),
