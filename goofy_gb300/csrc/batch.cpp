@@ -63,10 +63,8 @@ struct goofy_gpu_batch {
     std::vector<uint32_t> units_scratch;
 };
 
-namespace {
-
-int validate_and_fill(const goofy_gpu_image* images, uint32_t count, uint32_t unit_blocks, BatchImage* desc,
-                      uint32_t* first, uint32_t* total_units)
+int goofy_gpu::validate_and_fill(const goofy_gpu_image* images, uint32_t count, uint32_t unit_blocks,
+                                 BatchImage* desc, uint32_t* first, uint32_t* total_units)
 {
     uint64_t units = 0;
     for (uint32_t i = 0; i < count; ++i) {
@@ -101,6 +99,10 @@ int validate_and_fill(const goofy_gpu_image* images, uint32_t count, uint32_t un
     *total_units = (uint32_t)units;
     return GOOFY_OK;
 }
+
+namespace {
+
+using goofy_gpu::validate_and_fill;
 
 void free_slot(Slot& s)
 {

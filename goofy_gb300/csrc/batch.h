@@ -5,6 +5,8 @@
 
 #include <cstdint>
 
+struct goofy_gpu_image;  // include/goofy_gpu.h
+
 namespace goofy_gpu {
 
 // One image of a batch, as the persistent kernel reads it.  Filled and
@@ -58,6 +60,14 @@ struct InlineBatch {
 };
 cudaError_t launch_batch_tma_inline(const InlineBatch& batch, uint32_t n_images, uint32_t total_units,
                                     const BatchTile& tile, uint32_t ctas, cudaStream_t stream);
+
+// Checks `count` caller images (codec, sizes multiples of 4, non-null and
+// aligned buffers, stride) and fills their device descriptors, the first-unit
+// table (`first[i]` = desc[i].first_unit) and the total of work units of
+// `unit_blocks` blocks.  Empty images get no units.  Returns GOOFY_OK or the
+// status of the first bad image (with its message in the last error).
+int validate_and_fill(const goofy_gpu_image* images, uint32_t count, uint32_t unit_blocks, BatchImage* desc,
+                      uint32_t* first, uint32_t* total_units);
 
 // Enqueue the persistent batch kernel.  `work_counter` must read 0 when the
 // kernel starts; `first_unit[i]` is images[i].first_unit (ascending, [0] = 0).

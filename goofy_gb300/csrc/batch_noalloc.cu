@@ -9,8 +9,15 @@
 // scratch in one fixed-size file-scope device array instead; the array is part
 // of the library's module and is held on every GPU that loads the library
 // until the process exits.  Inputs and outputs are still the caller's device
-// buffers.  The kernel is the ordinary batch kernel, given pointers into the
-// array.
+// buffers.
+//
+// A call is two launches on the caller's stream: a one-CTA kernel that takes
+// the call's descriptor and first-unit tables as its by-value parameter,
+// writes them into the array and zeroes the work counter; then the ordinary
+// batch kernel, given pointers into the array.  No host-to-device copy is
+// made, so nothing is read from the calling thread's memory after the call
+// returns.
+#include <cuda.h>  // driver types for the context queries (entry points fetched at run time)
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -35,55 +42,112 @@ struct Scratch {
 // The whole scratch: 256 + 4 * 256 + 48 * 256 = 13,568 bytes per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(Scratch)];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-Scratch* g_scratch_addr[kMaxDevices] = {};
+// A call's tables as a kernel parameter: N descriptors and first units
+// (13,312 bytes for N = 256, within the 32,764-byte parameter limit).  Small
+// calls use the 32-image form, whose launch carries 1.7 KB.
+template <uint32_t N>
+struct Tables {
+    goofy_gpu::BatchImage images[N];
+    uint32_t first_unit[N];
+};
 
-// Device address of the scratch array on the current device.  The first call
-// per device asks the runtime for it (cudaGetSymbolAddress) and caches it.
+template <uint32_t N>
+__global__ void __launch_bounds__(256) noalloc_stage_kernel(const __grid_constant__ Tables<N> t, uint32_t count)
+{
+    Scratch* s = reinterpret_cast<Scratch*>(g_noalloc_scratch);
+    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+        s->images[i] = t.images[i];
+        s->first_unit[i] = t.first_unit[i];
+    }
+    if (threadIdx.x == 0) s->work_counter = 0u;  // the previous call left its final count here
+}
+
+// Unique id of the calling thread's current context (0 when none is current
+// or the driver lacks the queries).  Context ids are never reused within a
+// process, unlike context handles.
+unsigned long long current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+        cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+constexpr int kMaxDevices = 64;
+struct Resolved {
+    unsigned long long context_id = 0;
+    Scratch* addr = nullptr;
+};
+std::mutex g_setup_mu;
+Resolved g_resolved[kMaxDevices];
+
+// Device address of the scratch array in the current device's context.  The
+// first call in a context asks the runtime for it (cudaGetSymbolAddress) and
+// keeps it with that context's id; a later call in the same context reuses
+// it.  A reset device (cudaDeviceReset) or another context made current gets
+// a new id, so the address is looked up again instead of reusing one that
+// belongs to a destroyed or different context.
 int scratch_address(Scratch** out)
 {
     int dev = 0;
     GOOFY_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return goofy_gpu::fail(GOOFY_ERR_NO_DEVICE, "noalloc: device index too large");
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return goofy_gpu::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
-        g_scratch_addr[dev] = static_cast<Scratch*>(p);
+    unsigned long long id = current_context_id();
+    {
+        std::lock_guard<std::mutex> lk(g_setup_mu);
+        if (id != 0 && g_resolved[dev].context_id == id) {
+            *out = g_resolved[dev].addr;
+            return GOOFY_OK;
+        }
     }
-    *out = g_scratch_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the primary context current if none is
+    if (e != cudaSuccess || !p) return goofy_gpu::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+    id = current_context_id();
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    g_resolved[dev].context_id = id;  // 0 (no context queries): looked up again on every call
+    g_resolved[dev].addr = static_cast<Scratch*>(p);
+    *out = g_resolved[dev].addr;
     return GOOFY_OK;
 }
 
-// Descriptor of one image (same rules as goofy_gpu_batch_encode).
-int describe(const goofy_gpu_image& im, uint32_t unit_blocks, uint64_t* units, goofy_gpu::BatchImage* d)
+// Validates the images into tables of N entries, then (if there is work)
+// launches the staging kernel and the batch kernel on `st`.
+template <uint32_t N>
+int encode_with(const goofy_gpu_image* images, uint32_t count, cudaStream_t st)
 {
-    std::memset(d, 0, sizeof *d);
-    if (im.codec != GOOFY_CODEC_BC1 && im.codec != GOOFY_CODEC_ETC1S)
-        return goofy_gpu::fail(GOOFY_ERR_INVALID, "noalloc: bad codec");
-    if (im.width % 4) return goofy_gpu::fail(GOOFY_ERR_WIDTH, "noalloc: width % 4 != 0");
-    if (im.height % 4) return goofy_gpu::fail(GOOFY_ERR_HEIGHT, "noalloc: height % 4 != 0");
-    const uint64_t bw = im.width / 4, bh = im.height / 4;
-    if (bw * bh > 0x7fffffffull) return goofy_gpu::fail(GOOFY_ERR_TOO_LARGE, "noalloc: image too large");
-    d->first_unit = (uint32_t)*units;
-    if (bw == 0 || bh == 0) return GOOFY_OK;
-    if (!im.src || !im.dst) return goofy_gpu::fail(GOOFY_ERR_INVALID, "noalloc: null pointer");
-    if ((uint64_t)im.stride < 4ull * im.width) return goofy_gpu::fail(GOOFY_ERR_INVALID, "noalloc: stride");
-    const uintptr_t s = reinterpret_cast<uintptr_t>(im.src);
-    if (reinterpret_cast<uintptr_t>(im.dst) % 8 || s % 4 || im.stride % 4)
-        return goofy_gpu::fail(GOOFY_ERR_ALIGNMENT, "noalloc: alignment");
-    d->src = static_cast<const uint8_t*>(im.src);
-    d->dst = static_cast<uint8_t*>(im.dst);
-    d->stride = im.stride;
-    d->bw = (uint32_t)bw;
-    d->bh = (uint32_t)bh;
-    d->bw_magic = 0xffffffffu / (uint32_t)bw;
-    d->codec = (uint32_t)im.codec;
-    d->vec16 = (s % 16 == 0 && im.stride % 16 == 0) ? 1u : 0u;
-    *units += (bw * bh + unit_blocks - 1) / unit_blocks;
-    if (*units > 0x7fffffffull) return goofy_gpu::fail(GOOFY_ERR_TOO_LARGE, "noalloc: too many work units");
+    const goofy_gpu::BatchTile tile{128, 1, 256, 0};
+    Tables<N> t;  // on this thread's stack; the launch copies it
+    std::memset(&t, 0, sizeof t);
+    uint32_t units = 0;
+    int rc = goofy_gpu::validate_and_fill(images, count, tile.unit_blocks, t.images, t.first_unit, &units);
+    if (rc != GOOFY_OK || units == 0) return rc;  // nothing launched for an invalid or empty batch
+    Scratch* s = nullptr;
+    if ((rc = scratch_address(&s)) != GOOFY_OK) return rc;
+    noalloc_stage_kernel<N><<<1, 256, 0, st>>>(t, count);
+    GOOFY_CUDA_TRY(cudaGetLastError());
+    const uint64_t needed = ((uint64_t)units * 32 + tile.threads - 1) / tile.threads;
+    const uint64_t resident = (uint64_t)goofy_gpu::batch_resident_ctas(tile.threads, tile.bpt);
+    const uint32_t ctas = (uint32_t)(needed < resident ? needed : resident);
+    GOOFY_CUDA_TRY(goofy_gpu::launch_batch(s->images, count, s->first_unit, units, &s->work_counter, tile, ctas, st));
     return GOOFY_OK;
 }
 
@@ -99,32 +163,7 @@ extern "C" GOOFY_EXPORT int goofy_gpu_batch_encode_noalloc(const goofy_gpu_image
         return goofy_gpu::fail(GOOFY_ERR_TOO_LARGE, msg);
     }
     if (count == 0) return GOOFY_OK;
-    if (!images) return GOOFY_ERR_INVALID;
-    const goofy_gpu::BatchTile tile{128, 1, 256};
-    // Host copies of the tables live on this thread's stack (13 KB).
-    goofy_gpu::BatchImage desc[kMaxImages];
-    uint32_t first[kMaxImages];
-    uint64_t units = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-        const int rc = describe(images[i], tile.unit_blocks, &units, &desc[i]);
-        if (rc != GOOFY_OK) return rc;
-        first[i] = desc[i].first_unit;
-    }
-    if (units == 0) return GOOFY_OK;
-    Scratch* s = nullptr;
-    const int rc = scratch_address(&s);
-    if (rc != GOOFY_OK) return rc;
+    if (!images) return goofy_gpu::fail(GOOFY_ERR_INVALID, "goofy_gpu_batch_encode_noalloc: images is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // Pageable source: each copy returns once the bytes are staged, so the
-    // stack tables may go out of scope right after.
-    GOOFY_CUDA_TRY(cudaMemcpyAsync(s->images, desc, sizeof(goofy_gpu::BatchImage) * count, cudaMemcpyHostToDevice, st));
-    GOOFY_CUDA_TRY(cudaMemcpyAsync(s->first_unit, first, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, st));
-    // The previous call left its final count in the work counter: clear it.
-    GOOFY_CUDA_TRY(cudaMemsetAsync(&s->work_counter, 0, sizeof(uint32_t), st));
-    const uint64_t needed = (units * 32 + tile.threads - 1) / tile.threads;
-    const uint64_t resident = (uint64_t)goofy_gpu::batch_resident_ctas(tile.threads, tile.bpt);
-    const uint32_t ctas = (uint32_t)(needed < resident ? needed : resident);
-    GOOFY_CUDA_TRY(goofy_gpu::launch_batch(s->images, count, s->first_unit, (uint32_t)units, &s->work_counter, tile,
-                                           ctas, st));
-    return GOOFY_OK;
+    return count <= 32 ? encode_with<32>(images, count, st) : encode_with<kMaxImages>(images, count, st);
 }
