@@ -124,6 +124,17 @@ def _declare(lib):
         "goofy_gpu_host_free": (None, [_VP]),
         "goofy_gpu_get_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
         "goofy_gpu_set_tile": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(Tile)]),
+        "goofy_gpu_reset_tiles": (ctypes.c_int, []),
+        "goofy_gpu_autotune_pair": (ctypes.c_int, [_VP, _VP, _VP, _U32, _U32, _U32, _U32, ctypes.POINTER(Tile),
+                                                   ctypes.POINTER(Tile), ctypes.POINTER(ctypes.c_float)]),
+        "goofy_gpu_set_tile_cache_path": (ctypes.c_int, [ctypes.c_char_p]),
+        "goofy_gpu_get_tile_cache_path": (ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
+        "goofy_gpu_device_key": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_U32)]),
+        "goofy_gpu_tile_cache_store": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _U32, ctypes.c_int,
+                                                      ctypes.POINTER(Tile), ctypes.c_float]),
+        "goofy_gpu_tile_cache_lookup": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _U32, ctypes.c_int,
+                                                       ctypes.POINTER(Tile)]),
+        "goofy_gpu_load_tile_cache": (ctypes.c_int, [ctypes.c_int]),
         "goofy_gpu_autotune": (ctypes.c_int, [ctypes.c_int, _VP, _VP, _U32, _U32, _U32, _U32, ctypes.POINTER(Tile),
                                               ctypes.POINTER(ctypes.c_float)]),
         "goofy_gpu_batch_create": (ctypes.c_int, [ctypes.POINTER(_VP), _U32, ctypes.c_int]),
@@ -303,6 +314,56 @@ def set_tile(codec, threads_per_cta, blocks_per_thread, persistent=0):
     return lib().goofy_gpu_set_tile(codec, ctypes.byref(t))
 
 
+def reset_tiles():
+    """Back to the compiled default tiles; the tile cache is read again on the
+    next goofy_gpu_init or encode call."""
+    return lib().goofy_gpu_reset_tiles()
+
+
+def _enc(s):
+    return None if s is None else os.fsencode(s)
+
+
+def set_tile_cache_path(path):
+    """Use `path` as the tile cache ("" disables it, None restores
+    $GOOFY_TILE_CACHE / the per-user default)."""
+    return lib().goofy_gpu_set_tile_cache_path(_enc(path))
+
+
+def tile_cache_path():
+    n = lib().goofy_gpu_get_tile_cache_path(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib().goofy_gpu_get_tile_cache_path(buf, n + 1)
+    return os.fsdecode(buf.value)
+
+
+def device_key(device=0):
+    """(GPU name, SM count): the key of a device's tile cache entries."""
+    buf = ctypes.create_string_buffer(256)
+    sms = _U32()
+    rc = lib().goofy_gpu_device_key(device, buf, 256, ctypes.byref(sms))
+    if rc != OK:
+        raise RuntimeError("device_key: %s %s" % (status_string(rc), last_error()))
+    return buf.value.decode(), sms.value
+
+
+def tile_cache_store(path, gpu_name, sm_count, codec, tile, us):
+    t = Tile(*tile)
+    return lib().goofy_gpu_tile_cache_store(_enc(path), gpu_name.encode(), sm_count, codec, ctypes.byref(t), us)
+
+
+def tile_cache_lookup(path, gpu_name, sm_count, codec):
+    """The recorded tile (threads, blocks a thread, mode) or None."""
+    t = Tile()
+    rc = lib().goofy_gpu_tile_cache_lookup(_enc(path), gpu_name.encode(), sm_count, codec, ctypes.byref(t))
+    return (t.threads_per_cta, t.blocks_per_thread, t.persistent) if rc == OK else None
+
+
+def load_tile_cache(device=0):
+    """Install the cached tiles of `device` (codecs not set explicitly); the count installed."""
+    return lib().goofy_gpu_load_tile_cache(device)
+
+
 def pipeline_timeouts(reset=False):
     """Bulk-copy pipeline waits that gave up on the current device (0 when healthy)."""
     n = _U32()
@@ -330,6 +391,19 @@ def autotune(codec, dst, src, width, height, stride, reps=9):
     if rc != OK:
         raise RuntimeError("autotune failed: %s %s" % (status_string(rc), last_error()))
     return (t.threads_per_cta, t.blocks_per_thread, t.persistent), us.value
+
+
+def autotune_pair(dst_bc1, dst_etc1s, src, width, height, stride, reps=5):
+    """Tune both codecs for alternating BC1 / ETC1s calls on one image; installs
+    the pair.  Returns (bc1 tile, etc1s tile, mean microseconds of one pair)."""
+    t0, t1 = Tile(), Tile()
+    us = ctypes.c_float()
+    rc = lib().goofy_gpu_autotune_pair(_addr(dst_bc1), _addr(dst_etc1s), _addr(src), width, height, stride, reps,
+                                       ctypes.byref(t0), ctypes.byref(t1), ctypes.byref(us))
+    if rc != OK:
+        raise RuntimeError("autotune_pair failed: %s %s" % (status_string(rc), last_error()))
+    return ((t0.threads_per_cta, t0.blocks_per_thread, t0.persistent),
+            (t1.threads_per_cta, t1.blocks_per_thread, t1.persistent), us.value)
 
 
 def out_size(width, height):

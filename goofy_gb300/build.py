@@ -35,8 +35,8 @@ def _cuda_home():
 
 
 CU_SOURCES = ["encode_kernels.cu", "encode_tma.cu", "batch_kernels.cu", "batch_noalloc.cu", "decode_kernels.cu", "mips.cu"]
-CPP_SOURCES = ["capi.cpp", "batch.cpp", "server.cpp", "server_replay.cpp", "quality.cpp", "containers.cpp", "png.cpp"]
-HEADERS = ["block_codec.cuh", "block_decode.cuh", "device_io.cuh", "async_copy.cuh", "pdl.cuh", "kernels.h", "batch.h", "host_util.h", "decode.h"]
+CPP_SOURCES = ["capi.cpp", "tile_cache.cpp", "batch.cpp", "server.cpp", "server_replay.cpp", "quality.cpp", "containers.cpp", "png.cpp"]
+HEADERS = ["block_codec.cuh", "block_decode.cuh", "device_io.cuh", "async_copy.cuh", "pdl.cuh", "kernels.h", "batch.h", "host_util.h", "decode.h", "tile_cache.h"]
 
 
 def _stale(target, deps):

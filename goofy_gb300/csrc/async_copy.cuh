@@ -56,6 +56,14 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         : "memory");
 }
 
+// Asks L2 to fetch `bytes` (a multiple of 16, 16-byte aligned address) of
+// global memory.  A hint: nothing lands in the CTA, nothing completes on a
+// barrier, and L2 stays coherent with every later write to those lines.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ uint64_t global_ns()
 {
     uint64_t t;

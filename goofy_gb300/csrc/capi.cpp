@@ -25,6 +25,7 @@
 #include "../../include/goofy_tc_gpu.h"
 #include "host_util.h"
 #include "kernels.h"
+#include "tile_cache.h"
 
 namespace goofy_gpu {
 
@@ -59,14 +60,71 @@ using goofy_gpu::Tile;
 
 #define CUDA_TRY GOOFY_CUDA_TRY
 
-// BC1: register-loading grid; ETC1s and the two-codec pass: bulk-copy pipeline; 2 blocks a thread
-Tile g_tile[3] = {{128, 2, 0}, {512, 2, 2}, {512, 2, 2}};
+// Every codec on the bulk-copy pipeline, 512 compute threads, 2 blocks a thread.  For BC1 alone the
+// register-loading grid is as fast on some boxes (the autotuner picks per box), but the bulk-copy
+// kernel lets a BC1 launch and an ETC1s launch follow each other without a gap: both use one CTA of
+// the same size per SM, so the next launch's CTA takes an SM as soon as the last one leaves it.
+constexpr Tile kDefaultTile[3] = {{512, 2, 2}, {512, 2, 2}, {512, 2, 2}};
+Tile g_tile[3] = {kDefaultTile[0], kDefaultTile[1], kDefaultTile[2]};
+bool g_tile_explicit[3] = {false, false, false};  // set by goofy_gpu_set_tile / the autotuner: the cache leaves it
 std::mutex g_tile_mu;
+constexpr int kMaxDevices = 64;
+std::atomic<bool> g_cache_loaded[kMaxDevices];
 
 Tile tile_for(int codec)
 {
     std::lock_guard<std::mutex> lk(g_tile_mu);
     return g_tile[codec == GOOFY_CODEC_BOTH ? 2 : codec & 1];
+}
+
+// Name and SM count of a device: the key of its tile cache entries.
+int device_key(int dev, std::string* name, uint32_t* sms)
+{
+    cudaDeviceProp p;
+    CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    *name = p.name;
+    *sms = (uint32_t)p.multiProcessorCount;
+    return GOOFY_OK;
+}
+
+// Installs the cached tiles of device `dev` for the codecs nobody set
+// explicitly; returns how many were installed, or a negative status.
+int load_tile_cache(int dev)
+{
+    std::string name;
+    uint32_t sms = 0;
+    const int rc = device_key(dev, &name, &sms);
+    if (rc != GOOFY_OK) return rc;
+    const std::string path = goofy_gpu::tile_cache_path();
+    Tile found[3];
+    bool have[3];
+    for (int c = 0; c < 3; ++c) have[c] = goofy_gpu::tile_cache_lookup(path, name, sms, c, &found[c]);
+    int applied = 0;
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    for (int c = 0; c < 3; ++c)
+        if (have[c] && !g_tile_explicit[c]) {
+            g_tile[c] = found[c];
+            ++applied;
+        }
+    if (dev >= 0 && dev < kMaxDevices) g_cache_loaded[dev].store(true);
+    return applied;
+}
+
+// Once per device and process (goofy_gpu_init, or the first encode call).
+void ensure_tile_cache(int dev)
+{
+    if (dev < 0 || dev >= kMaxDevices || g_cache_loaded[dev].load(std::memory_order_relaxed)) return;
+    if (load_tile_cache(dev) < 0) {
+        cudaGetLastError();
+        g_cache_loaded[dev].store(true);  // no usable entry: keep the compiled defaults
+    }
+}
+
+void ensure_tile_cache_current()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) ensure_tile_cache(dev);
+    else cudaGetLastError();
 }
 
 struct Buffer {
@@ -223,6 +281,7 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
     }
     DeviceGuard g(hp.device);
     CUDA_TRY(g.err);
+    ensure_tile_cache(hp.device);
 
     // Direct path: one kernel reads the caller's rows and writes its blocks
     // over the host link, no staging copies.
@@ -236,9 +295,10 @@ int compress_host_impl(int codec, uint8_t* dst, const uint8_t* src, uint32_t wid
                              reinterpret_cast<uintptr_t>(ddst2) % 8 == 0;
         if (dsrc && ddst && (!both || ddst2) && aligned) {
             const SrcAccess access = (sa % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
-            // bulk async copies only ever read device memory: host rows go through the register-loading kernel
+            // bulk async copies only ever read device memory: host rows go through the register-loading
+            // kernel, in CTAs of 128 threads, whose number spreads the host-link reads over every SM
             Tile t = tile_for(codec);
-            if (t.persistent == 2) t.persistent = 0;
+            if (t.persistent == 2) t = Tile{128, t.bpt, 0};
             CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(dsrc), stride,
                                              static_cast<uint8_t*>(ddst), width, height, t, access, hp.stream[0],
                                              static_cast<uint8_t*>(ddst2)));
@@ -320,6 +380,7 @@ int compress_device_impl(int codec, void* dst, const void* src, uint32_t width, 
     if (s % 16 == 0 && stride % 16 == 0) access = SrcAccess::kVec16;
     else if (s % 4 == 0 && stride % 4 == 0) access = SrcAccess::kWord4;
     else return GOOFY_ERR_ALIGNMENT;
+    ensure_tile_cache_current();
     CUDA_TRY(goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
                                      width, height, tile_for(codec), access, static_cast<cudaStream_t>(stream)));
     return GOOFY_OK;
@@ -338,10 +399,96 @@ int compress_both_device_impl(void* dst_bc1, void* dst_etc1s, const void* src, u
     if (s % 16 == 0 && stride % 16 == 0) access = SrcAccess::kVec16;
     else if (s % 4 == 0 && stride % 4 == 0) access = SrcAccess::kWord4;
     else return GOOFY_ERR_ALIGNMENT;
+    ensure_tile_cache_current();
     CUDA_TRY(goofy_gpu::launch_image(GOOFY_CODEC_BOTH, static_cast<const uint8_t*>(src), stride,
                                      static_cast<uint8_t*>(dst_bc1), width, height, tile_for(GOOFY_CODEC_BOTH), access,
                                      static_cast<cudaStream_t>(stream), static_cast<uint8_t*>(dst_etc1s)));
     return GOOFY_OK;
+}
+
+// Times launches for the autotuners on a stream of their own: after two
+// warm-up launches, three rounds of `reps` launches back to back between two
+// events (an event between two launches would delay the second one's start);
+// `ms` is the median round's mean time of one launch(k).
+struct Timer {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+
+    int init()
+    {
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+        return GOOFY_OK;
+    }
+
+    ~Timer()
+    {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <typename F>
+    cudaError_t time(uint32_t reps, float& ms, F launch)
+    {
+        float t[3];
+        cudaError_t e = cudaSuccess;
+        for (uint32_t w = 0; w < 2 && e == cudaSuccess; ++w) e = launch(w);
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(ev[0], stream);
+            for (uint32_t k = 0; k < reps && e == cudaSuccess; ++k) e = launch(k);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], ev[0], ev[1]);
+            t[r] /= (float)reps;
+        }
+        std::sort(t, t + 3);
+        ms = t[1];
+        return e;
+    }
+};
+
+// Every tile shape of `codec`, fastest first, as (mean ms a launch, tile).
+int rank_tiles(Timer& tm, int codec, uint8_t* dst, uint8_t* dst2, const uint8_t* src, uint32_t stride,
+               uint32_t width, uint32_t height, SrcAccess access, uint32_t reps,
+               std::vector<std::pair<float, Tile>>* ranked)
+{
+    const bool both = codec == GOOFY_CODEC_BOTH;
+    ranked->clear();
+    for (uint32_t persistent : {0u, 1u, 2u})
+        for (uint32_t threads : {128u, 256u, 512u})
+            for (uint32_t bpt : {1u, 2u, 4u}) {
+                const Tile t{threads, bpt, persistent};
+                if (!goofy_gpu::tile_valid(t) || (both && (bpt > 2 || persistent == 1))) continue;
+                float ms = 0.f;
+                const cudaError_t e = tm.time(reps, ms, [&](uint32_t) {
+                    return goofy_gpu::launch_image(codec, src, stride, dst, width, height, t, access, tm.stream, dst2);
+                });
+                if (e != cudaSuccess) return cuda_fail(e, "autotune launch");
+                ranked->emplace_back(ms, t);
+            }
+    std::stable_sort(ranked->begin(), ranked->end(),
+                     [](const std::pair<float, Tile>& a, const std::pair<float, Tile>& b) { return a.first < b.first; });
+    return GOOFY_OK;
+}
+
+// Installs a tuned tile as the codec's (an explicit setting) and records it
+// for this GPU model; a cache that cannot be written keeps the result valid
+// for this process.
+void install_and_record(int codec, const Tile& t, float ms)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        g_tile[codec] = t;
+        g_tile_explicit[codec] = true;
+    }
+    int dev = 0;
+    std::string name;
+    uint32_t sms = 0;
+    const std::string path = goofy_gpu::tile_cache_path();
+    if (!path.empty() && cudaGetDevice(&dev) == cudaSuccess && device_key(dev, &name, &sms) == GOOFY_OK)
+        goofy_gpu::tile_cache_store(path, name, sms, codec, t, ms > 0.f ? ms * 1e3f : 1.f);
+    cudaGetLastError();
 }
 
 }  // namespace
@@ -352,7 +499,9 @@ GOOFY_EXPORT int goofy_gpu_init(int device)
 {
     HostPath& hp = host_path();
     std::lock_guard<std::mutex> lk(hp.mu);
-    return hp.init_locked(device);
+    const int rc = hp.init_locked(device);
+    if (rc == GOOFY_OK) ensure_tile_cache(device);
+    return rc;
 }
 
 GOOFY_EXPORT void goofy_gpu_shutdown(void)
@@ -472,8 +621,74 @@ GOOFY_EXPORT int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile)
     if (!goofy_gpu::tile_valid(t) || (codec == GOOFY_CODEC_BOTH && t.bpt > 2)) return GOOFY_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_tile_mu);
     g_tile[codec] = t;
+    g_tile_explicit[codec] = true;
     return GOOFY_OK;
 }
+
+GOOFY_EXPORT int goofy_gpu_reset_tiles(void)
+{
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    for (int c = 0; c < 3; ++c) {
+        g_tile[c] = kDefaultTile[c];
+        g_tile_explicit[c] = false;
+    }
+    for (auto& f : g_cache_loaded) f.store(false);
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_set_tile_cache_path(const char* path)
+{
+    goofy_gpu::set_tile_cache_path(path);
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT size_t goofy_gpu_get_tile_cache_path(char* buf, size_t size)
+{
+    const std::string p = goofy_gpu::tile_cache_path();
+    if (buf && size) {
+        const size_t n = std::min(size - 1, p.size());
+        std::memcpy(buf, p.data(), n);
+        buf[n] = '\0';
+    }
+    return p.size();
+}
+
+GOOFY_EXPORT int goofy_gpu_device_key(int device, char* name, size_t size, uint32_t* sm_count)
+{
+    if (!name || size == 0 || !sm_count) return GOOFY_ERR_INVALID;
+    std::string n;
+    const int rc = device_key(device, &n, sm_count);
+    if (rc != GOOFY_OK) return rc;
+    const size_t k = std::min(size - 1, n.size());
+    std::memcpy(name, n.data(), k);
+    name[k] = '\0';
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_tile_cache_store(const char* path, const char* gpu_name, uint32_t sm_count, int codec,
+                                            const goofy_gpu_tile* tile, float us)
+{
+    if (!gpu_name || !tile) return GOOFY_ERR_INVALID;
+    const Tile t{tile->threads_per_cta, tile->blocks_per_thread, tile->persistent};
+    return goofy_gpu::tile_cache_store(path ? std::string(path) : goofy_gpu::tile_cache_path(), gpu_name, sm_count,
+                                       codec, t, us);
+}
+
+GOOFY_EXPORT int goofy_gpu_tile_cache_lookup(const char* path, const char* gpu_name, uint32_t sm_count, int codec,
+                                             goofy_gpu_tile* tile)
+{
+    if (!gpu_name || !tile) return GOOFY_ERR_INVALID;
+    Tile t{0, 0, 0};
+    if (!goofy_gpu::tile_cache_lookup(path ? std::string(path) : goofy_gpu::tile_cache_path(), gpu_name, sm_count,
+                                      codec, &t))
+        return goofy_gpu::fail(GOOFY_ERR_INVALID, "tile cache: no entry");
+    tile->threads_per_cta = t.threads;
+    tile->blocks_per_thread = t.bpt;
+    tile->persistent = t.persistent;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_load_tile_cache(int device) { return load_tile_cache(device); }
 
 GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height,
                                    uint32_t stride, uint32_t reps, goofy_gpu_tile* best, float* best_us)
@@ -485,65 +700,86 @@ GOOFY_EXPORT int goofy_gpu_autotune(int codec, void* dst, const void* src, uint3
     const uintptr_t s = reinterpret_cast<uintptr_t>(src);
     if (reinterpret_cast<uintptr_t>(dst) % 8 != 0 || s % 4 != 0 || stride % 4 != 0) return GOOFY_ERR_ALIGNMENT;
     const SrcAccess access = (s % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    int result = GOOFY_OK;
-    Tile best_tile{0, 0, 0};
-    float best_time = 0.f;
-    std::vector<float> times(3);
-    for (int i = 0; i < 2 && result == GOOFY_OK; ++i)
-        if (cudaEventCreate(&ev[i]) != cudaSuccess) result = cuda_fail(cudaGetLastError(), "cudaEventCreate");
-    std::vector<Tile> candidates;
-    for (uint32_t persistent : {0u, 1u, 2u})
-        for (uint32_t threads : {128u, 256u, 512u})
-            for (uint32_t bpt : {1u, 2u, 4u})
-                if (goofy_gpu::tile_valid(Tile{threads, bpt, persistent}) && !(both && (bpt > 2 || persistent == 1)))
-                    candidates.push_back(Tile{threads, bpt, persistent});
+    Timer tm;
+    if ((rc = tm.init()) != GOOFY_OK) return rc;
     uint8_t* const dst2 = both ? static_cast<uint8_t*>(dst) + (size_t)(width / 4) * (height / 4) * 8 : nullptr;
-    for (const Tile& t : candidates) {
-        if (result != GOOFY_OK) break;
-        auto launch = [&] {
-            return goofy_gpu::launch_image(codec, static_cast<const uint8_t*>(src), stride, static_cast<uint8_t*>(dst),
-                                           width, height, t, access, st, dst2);
-        };
-        // three rounds of `reps` launches back to back between two events (an
-        // event between two launches would delay the second one's start); the
-        // median round's mean launch time
-        cudaError_t e = cudaSuccess;
-        for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = launch();
-        for (uint32_t r = 0; r < 3 && e == cudaSuccess; ++r) {
-            e = cudaEventRecord(ev[0], st);
-            for (uint32_t k = 0; k < reps && e == cudaSuccess; ++k) e = launch();
-            if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
-            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&times[r], ev[0], ev[1]);
-            times[r] /= (float)reps;
-        }
-        if (e != cudaSuccess) {
-            result = cuda_fail(e, "autotune launch");
-            break;
-        }
-        std::sort(times.begin(), times.end());
-        const float med = times[1];
-        if (best_tile.threads == 0 || med < best_time) {
-            best_time = med;
-            best_tile = t;
-        }
-    }
-    for (auto& e : ev)
-        if (e) cudaEventDestroy(e);
-    cudaStreamDestroy(st);
-    if (result != GOOFY_OK) return result;
-    {
-        std::lock_guard<std::mutex> lk(g_tile_mu);
-        g_tile[codec] = best_tile;
-    }
+    std::vector<std::pair<float, Tile>> ranked;
+    if ((rc = rank_tiles(tm, codec, static_cast<uint8_t*>(dst), dst2, static_cast<const uint8_t*>(src), stride,
+                         width, height, access, reps, &ranked)) != GOOFY_OK)
+        return rc;
+    const Tile best_tile = ranked[0].second;
+    const float best_time = ranked[0].first;
+    install_and_record(codec, best_tile, best_time);
     if (best) {
         best->threads_per_cta = best_tile.threads;
         best->blocks_per_thread = best_tile.bpt;
         best->persistent = best_tile.persistent;
     }
+    if (best_us) *best_us = best_time * 1e3f;
+    return GOOFY_OK;
+}
+
+GOOFY_EXPORT int goofy_gpu_autotune_pair(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width,
+                                        uint32_t height, uint32_t stride, uint32_t reps, goofy_gpu_tile* best_bc1,
+                                        goofy_gpu_tile* best_etc1s, float* best_us)
+{
+    int rc = check_args(GOOFY_CODEC_BC1, dst_bc1, src, width, height, stride);
+    if (rc <= 0) return rc == GOOFY_OK ? GOOFY_ERR_INVALID : rc;
+    if (!dst_etc1s || outputs_overlap(dst_bc1, dst_etc1s, width, height)) return GOOFY_ERR_INVALID;
+    if (reps == 0 || reps > 1000) return GOOFY_ERR_INVALID;
+    const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+    if (reinterpret_cast<uintptr_t>(dst_bc1) % 8 || reinterpret_cast<uintptr_t>(dst_etc1s) % 8 || s % 4 ||
+        stride % 4)
+        return GOOFY_ERR_ALIGNMENT;
+    const SrcAccess access = (s % 16 == 0 && stride % 16 == 0) ? SrcAccess::kVec16 : SrcAccess::kWord4;
+    const uint8_t* in = static_cast<const uint8_t*>(src);
+    uint8_t* out[2] = {static_cast<uint8_t*>(dst_bc1), static_cast<uint8_t*>(dst_etc1s)};
+    Timer tm;
+    if ((rc = tm.init()) != GOOFY_OK) return rc;
+    // each codec alone first; the pairs of each codec's kFinalists fastest shapes then run as the
+    // alternating BC1 / ETC1s sequence a caller encoding every image with both codecs issues
+    constexpr size_t kFinalists = 4;
+    std::vector<std::pair<float, Tile>> ranked[2];
+    for (int c = 0; c < 2; ++c)
+        if ((rc = rank_tiles(tm, c, out[c], nullptr, in, stride, width, height, access, reps, &ranked[c])) !=
+            GOOFY_OK)
+            return rc;
+    Tile best[2] = {ranked[0][0].second, ranked[1][0].second};
+    float best_time = -1.f;
+    for (size_t i = 0; i < std::min(kFinalists, ranked[0].size()); ++i)
+        for (size_t j = 0; j < std::min(kFinalists, ranked[1].size()); ++j) {
+            const Tile t[2] = {ranked[0][i].second, ranked[1][j].second};
+            float ms = 0.f;
+            const cudaError_t e = tm.time(reps, ms, [&](uint32_t k) -> cudaError_t {
+                cudaError_t r = goofy_gpu::launch_image(GOOFY_CODEC_BC1, in, stride, out[0], width, height, t[0],
+                                                        access, tm.stream);
+                (void)k;
+                return r == cudaSuccess ? goofy_gpu::launch_image(GOOFY_CODEC_ETC1S, in, stride, out[1], width,
+                                                                  height, t[1], access, tm.stream)
+                                        : r;
+            });
+            if (e != cudaSuccess) return cuda_fail(e, "autotune pair launch");
+            if (best_time < 0.f || ms < best_time) {
+                best_time = ms;
+                best[0] = t[0];
+                best[1] = t[1];
+            }
+        }
+    for (int c = 0; c < 2; ++c) {
+        float alone = 0.f;
+        for (const auto& r : ranked[c])
+            if (r.second.threads == best[c].threads && r.second.bpt == best[c].bpt &&
+                r.second.persistent == best[c].persistent)
+                alone = r.first;
+        install_and_record(c, best[c], alone);
+    }
+    goofy_gpu_tile* const want[2] = {best_bc1, best_etc1s};
+    for (int c = 0; c < 2; ++c)
+        if (want[c]) {
+            want[c]->threads_per_cta = best[c].threads;
+            want[c]->blocks_per_thread = best[c].bpt;
+            want[c]->persistent = best[c].persistent;
+        }
     if (best_us) *best_us = best_time * 1e3f;
     return GOOFY_OK;
 }

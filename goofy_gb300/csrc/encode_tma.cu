@@ -96,7 +96,26 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     }
     if constexpr (CODEC != kBC1) fill_ctrl_lut(ctrl_lut);
     __syncthreads();
-    pdl_wait();  // no global memory before the previous kernel in the stream is done
+#ifndef GOOFY_L2_PREFETCH_TILES
+#define GOOFY_L2_PREFETCH_TILES L.stages
+#endif
+    if (warp == compute_warps && lane == 0) {
+        // While the previous kernel in the stream drains, ask L2 for the rows
+        // of this CTA's first tiles.  Only a hint: no data enters the CTA
+        // before pdl_wait(), and L2 is coherent with the previous kernel's
+        // writes, so the copies after the wait still read what it wrote.
+        uint32_t n = 0;
+        for (uint32_t t = blockIdx.x; t < total_tiles && n < (GOOFY_L2_PREFETCH_TILES); t += gridDim.x, ++n) {
+            uint32_t tx;
+            const uint32_t by = div_magic(t, tiles_per_row, tile_magic, tx);
+            const uint32_t bx0 = tx * L.tile_blocks;
+            const uint32_t bytes = 16u * min(L.tile_blocks, bw - bx0);
+            const uint8_t* row = src + (size_t)by * 4u * stride + 16u * (size_t)bx0;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) bulk_prefetch_l2(row + r * stride, bytes);
+        }
+    }
+    pdl_wait();  // no global memory access before the previous kernel in the stream is done
 
     if (warp == compute_warps) {  // producer
         if (lane != 0) return;

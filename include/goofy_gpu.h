@@ -144,7 +144,8 @@ typedef struct goofy_gpu_tile {
 
 /* Get / set the tile the image kernels launch with, per codec
  * (GOOFY_CODEC_BOTH: the two-codec pass; 1 or 2 blocks a thread, and mode 1
- * runs as mode 0 there). */
+ * runs as mode 0 there).  Compiled default for every codec: 512 threads,
+ * 2 blocks a thread, mode 2. */
 int goofy_gpu_get_tile(int codec, goofy_gpu_tile* tile);
 int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
 
@@ -158,6 +159,56 @@ int goofy_gpu_set_tile(int codec, const goofy_gpu_tile* tile);
  * (2 * (width/4)(height/4)*8 bytes, the BC1 blocks first). */
 int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, uint32_t height, uint32_t stride,
                        uint32_t reps, goofy_gpu_tile* best, float* best_us);
+
+/* Autotuner for callers that encode every image with both codecs, one call
+ * after the other (as the reference harness calls goofy::compressDXT1 and
+ * goofy::compressETC1 on each image): ranks each codec's tiles alone as
+ * goofy_gpu_autotune does, then times the alternating BC1 / ETC1s launches for
+ * the pairs of each codec's four fastest tiles -- a shape that is fastest
+ * alone can leave a gap where the other codec's launch takes over the SMs --
+ * and installs the fastest pair.  best_us: the mean time of one BC1 + ETC1s
+ * pair.  Both outputs (dst_bc1, dst_etc1s) must not overlap.  Synchronous.  No
+ * reference counterpart. */
+int goofy_gpu_autotune_pair(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width, uint32_t height,
+                            uint32_t stride, uint32_t reps, goofy_gpu_tile* best_bc1, goofy_gpu_tile* best_etc1s,
+                            float* best_us);
+
+/* ---- tile cache: tuned tiles kept per GPU model --------------------------- */
+/* No reference counterpart (the reference has no launch shape to tune).  The
+ * fastest tile differs between boxes of the same GPU model, so
+ * goofy_gpu_autotune records its pick in a text file keyed by GPU name and SM
+ * count, and goofy_gpu_init -- or, without it, a process's first encode call
+ * (the drop-in goofy::compressDXT1 / compressETC1 included) -- installs the
+ * recorded tile of every codec whose tile was not set explicitly
+ * (goofy_gpu_set_tile, goofy_gpu_autotune).  Without an entry the compiled
+ * defaults stay.  Tiles are process-wide, not per device: with several GPU
+ * models in one process the last one loaded wins.
+ * File: the path given to goofy_gpu_set_tile_cache_path, else
+ * $GOOFY_TILE_CACHE ("" disables the cache), else
+ * $XDG_CACHE_HOME/goofy_gb300/tiles.txt, else $HOME/.cache/goofy_gb300/tiles.txt.
+ * One entry per line, "v1|<GPU name>|<SM count>|<bc1|etc1s|both>|<threads>|
+ * <blocks a thread>|<mode>|<microseconds>"; lines that do not parse, name a
+ * tile the kernels cannot run or belong to another GPU model are ignored.  A
+ * write replaces the file atomically (temporary file + rename); a cache that
+ * cannot be written leaves the autotuner's result in effect for the process. */
+int goofy_gpu_set_tile_cache_path(const char* path); /* NULL: back to the environment / default */
+/* The path in use; copies at most size-1 bytes and a NUL into buf (may be
+ * NULL) and returns the full length. */
+size_t goofy_gpu_get_tile_cache_path(char* buf, size_t size);
+/* The GPU name and SM count that key `device`'s entries. */
+int goofy_gpu_device_key(int device, char* name, size_t size, uint32_t* sm_count);
+/* Record / look up one entry directly (path NULL: the path in use).  Need no
+ * GPU.  lookup returns GOOFY_ERR_INVALID when there is no valid entry. */
+int goofy_gpu_tile_cache_store(const char* path, const char* gpu_name, uint32_t sm_count, int codec,
+                               const goofy_gpu_tile* tile, float us);
+int goofy_gpu_tile_cache_lookup(const char* path, const char* gpu_name, uint32_t sm_count, int codec,
+                                goofy_gpu_tile* tile);
+/* Installs `device`'s cached tiles now (codecs not set explicitly); returns
+ * how many were installed, or a negative status. */
+int goofy_gpu_load_tile_cache(int device);
+/* Restores the compiled default tiles and forgets which were set explicitly;
+ * the cache is read again by the next goofy_gpu_init or encode call. */
+int goofy_gpu_reset_tiles(void);
 
 /* Waits of the bulk-copy pipeline (tile mode 2) that gave up after their
  * time limit on the current device (each ends its kernel early instead of
@@ -419,13 +470,18 @@ int goofy_gpu_plain_replay(int device, const goofy_gpu_request* reqs, const int6
  * The work counter and descriptor tables live in one fixed file-scope device
  * array of the library (13,568 bytes, held on every GPU that loads the library
  * until the process exits), so a call takes at most GOOFY_NOALLOC_MAX_IMAGES
- * images; more returns GOOFY_ERR_TOO_LARGE.  The caller's images (device
- * src / dst) are the inputs and outputs.  The first call on a device looks up
- * the array's device address with cudaGetSymbolAddress; make that first call
- * before any stream capture.  All calls share the array: calls whose GPU work
- * overlaps (e.g. on two unordered streams) race; issue them on one stream or
- * order them.  Asynchronous on `stream` (the descriptor copy is staged from
- * the calling thread's stack before the function returns). */
+ * images; more returns GOOFY_ERR_TOO_LARGE, a NULL `images` with count > 0
+ * GOOFY_ERR_INVALID, and an invalid image its status -- all before anything
+ * is launched.  The caller's images (device src / dst) are the inputs and
+ * outputs; they must be on the calling thread's current device, whose copy of
+ * the array the call uses.  The first call in a context (a device's primary
+ * context, again after cudaDeviceReset) looks up the array's device address
+ * with cudaGetSymbolAddress; make that first call before any stream capture.
+ * All calls share the array: calls whose GPU work overlaps (e.g. on two
+ * unordered streams) race; issue them on one stream or order them.
+ * Asynchronous on `stream`: two launches, a small kernel that takes the
+ * call's tables as its parameter and writes them into the array, then the
+ * batch kernel; no host memory is read after the call returns. */
 int goofy_gpu_batch_encode_noalloc(const goofy_gpu_image* images, uint32_t count, void* stream);
 
 #ifdef __cplusplus

@@ -10,6 +10,10 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "goofy_golden.npz")
 
+# Tests run with the compiled default tiles: no tuned tiles from a per-user
+# cache file of an earlier run.  The tile-cache tests give their own paths.
+os.environ.setdefault("GOOFY_TILE_CACHE", "")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
