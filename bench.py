@@ -21,8 +21,11 @@ previous launch did not touch (inputs larger than the 129 MB L2).
 * cpu_baseline -- the oracle port timed on this host's cores (bounded sample).
 * both_codecs_one_pass -- beside the headline: the same two outputs from one
                 read of the image (goofy_gpu_compress_both_*), device and host.
-* cold_configs -- the 256x256 scene and the 4096x4096 stress image, each
-                launch timed alone with L2 flushed before it.
+* small_configs -- the 4096x4096 stress image (launches back to back over
+                inputs rotating through 256 MiB) and the 256x256 scene
+                (latency of one launch with L2 cold).
+* summary    -- the figures above that the other sections explain, in one
+                short object at the end of the line.
 
 ``--impl reference`` times the reference's CPU implementation of the path on
 this host's cores instead (the reference compiled from its own sources where
@@ -217,18 +220,15 @@ def cpu_model():
 
 
 def cpu_baseline(img, gpu_outputs, budget_s=12.0):
-    """Oracle port (or the compiled reference where present) on this host's
-    cores: all threads, best of a few full-image passes of both codecs.  The
-    CPU outputs of the last pass double as the check of the GPU outputs."""
+    """The reference's own CPU encoder (its SSE2 path on x86-64, its scalar
+    path elsewhere; the oracle port only where neither was built) on this
+    host's cores: all threads, best of a few full-image passes of both codecs.
+    The CPU outputs of the last pass double as the check of the GPU outputs."""
     import numpy as np
 
     import oracle
 
-    ref = oracle.load_ref()
-    if ref is not None:
-        fn, kind = ref.ref_compress_mt, "reference"
-    else:
-        fn, kind = oracle.load().oracle_compress_mt, "port"
+    fn, kind, label = oracle.ref_encoder()
     cores = os.cpu_count() or 1
     times = []
     outs = [np.empty((W // 4) * (H // 4) * 8, np.uint8) for _ in range(2)]
@@ -245,7 +245,7 @@ def cpu_baseline(img, gpu_outputs, budget_s=12.0):
                       % (len(times), cores),
             "single_thread_mpix_s": round(px / t1 / 1e6, 1),
             "median_mpix_s": round(px / statistics.median(times) / 1e6, 1),
-            "cpu": "%s, %s" % (cpu_model(), platform.machine()),
+            "implementation": label, "cpu": "%s, %s" % (cpu_model(), platform.machine()),
             "gpu_output_bit_exact": bool(all(np.array_equal(outs[c], gpu_outputs[c]) for c in (0, 1)))}
 
 
@@ -277,43 +277,130 @@ def run_dropin_latency(g, img, sides=(256, 1024, 4096), calls=50):
     return res
 
 
-def run_cold_configs(g, torch, workloads, codecs, stream, reps=20):
-    """The two other single-image workloads, timed cold: the 256x256 scene
-    (seed 0, launch-latency bound, L2-resident once warm) and the 4096x4096
-    stress quarters (seed 2).  Before each launch a 256 MiB buffer is written,
-    which leaves none of the image in the 129 MB L2; each launch is bracketed
-    by its own two CUDA events.  Median and min of `reps` launches."""
-    sh = stream.cuda_stream
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=stream.device)
-    cases = [("256x256 scene (seed 0, stride 1024 B)", 256, workloads.scene(256, 256, 0)),
-             ("4096x4096 stress quarters (seed 2: uniform noise, constant blocks, two-colour blocks, grey with "
-              "random alpha)", 4096, workloads.stress(4096, 4096, 2))]
-    out = {}
-    for name, side, img in cases:
-        src = torch.from_numpy(img.reshape(-1)).to(stream.device)
-        dst = torch.empty(g.out_size(side, side), dtype=torch.uint8, device=stream.device)
-        row = {"workload": name}
-        for c in codecs:
-            ts = []
-            for r in range(reps + 2):
-                flush.fill_(r & 0xff)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                rc = g.compress_device(c, dst.data_ptr(), src.data_ptr(), side, side, 4 * side, sh)
-                e1.record(stream)
-                if rc != g.OK:
-                    raise RuntimeError("%s: %s" % (name, g.last_error()))
-                e1.synchronize()
-                if r >= 2:
-                    ts.append(e0.elapsed_time(e1) * 1e3)
-            med = statistics.median(ts)
-            row["bc1" if c == g.CODEC_BC1 else "etc1s"] = {
-                "median_us": round(med, 2), "min_us": round(min(ts), 2),
-                "mpix_s": round(side * side / med, 1), "hbm_gbs": round(ALG_BYTES_PER_PX * side * side / med / 1e3, 1)}
-        out["%dx%d" % (side, side)] = row
-    out["timing"] = ("each launch between its own two CUDA events after a 256 MiB write (L2 cold), %d launches "
-                     "after 2 untimed ones, default tiles" % reps)
+def summary(line, peak):
+    """The figures of the line in one short flat object (the line's last key)."""
+    def get(*path):
+        d = line
+        for k in path:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    out = {"step_us": round(1e3 * line["ms_per_step"], 2),
+           "bc1_8192_us": get("per_codec", "bc1", "mean_launch_us"),
+           "etc1s_8192_us": get("per_codec", "etc1s", "mean_launch_us"),
+           "step_frac": round(ALG_BYTES_PER_PX * line["config"]["pixels_per_step"] / (line["ms_per_step"] * 1e-3)
+                              / 1e9 / peak, 4),
+           "dominant_frac": get("roofline", "frac"),
+           "tiles": get("config", "tiles"), "cached_tiles_step_ratio": get("tile_cache", "cached_over_tuned"),
+           "stress4096_bc1_us": get("small_configs", "4096x4096", "bc1", "mean_launch_us"),
+           "stress4096_etc1s_us": get("small_configs", "4096x4096", "etc1s", "mean_launch_us"),
+           "stress4096_bc1_frac": get("small_configs", "4096x4096", "bc1", "frac"),
+           "stress4096_etc1s_frac": get("small_configs", "4096x4096", "etc1s", "frac"),
+           "scene256_latency_us": [get("small_configs", "256x256", c, "latency_us") for c in ("bc1", "etc1s")],
+           "both_one_pass_us": get("both_codecs_one_pass", "mean_launch_us"),
+           "batched_speedup_vs_plain": get("batched", "speedup_vs_plain"),
+           "batched_mpix_s": get("batched", "batched_mpix_s"),
+           "e2e_mpix_s": get("e2e", "value"),
+           "cpu_mpix_s": get("cpu_baseline", "value"), "cpu_kind": get("cpu_baseline", "kind")}
+    for mode in ("staged", "direct"):
+        l50 = get("serving", mode, "loads", "50%")
+        if l50:
+            out["serve_%s_50pct_p99_ms" % mode] = l50["p99_ms"]
+            out["serve_%s_50pct_probe_p99_ms" % mode] = get("serving", mode, "loads", "50%", "by_class",
+                                                            "probe_1024x1024", "p99_ms")
+    out["serve_vs_plain"] = get("serving", "plain", "server_vs_plain")
     return out
+
+
+def back_to_back_us(torch, stream, launch, n, rounds=3):
+    """Mean duration of one launch: `n` launches back to back between two CUDA
+    events on `stream` (no event between two launches), median of `rounds`
+    rounds after two untimed launches.  launch(k) enqueues launch k."""
+    for k in range(2):
+        launch(k)
+    ts = []
+    for _ in range(rounds):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(n):
+            launch(k)
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e3 / n)
+    return statistics.median(ts)
+
+
+def run_small_configs(args, g, torch, workloads, codecs, stream, peak):
+    """The two other single-image workloads.
+
+    * 4096x4096 stress quarters (seed 2): each codec as launches back to back
+      between two CUDA events, the input rotating over 4 device copies of the
+      64 MiB image (256 MiB, twice the L2) and the output over 4 buffers, so
+      no launch finds its input in L2.  Mean launch time and the fraction of
+      the measured HBM peak at 4.5 B/px.  Also the alternating BC1 / ETC1s
+      pair, as a caller encoding the image with both codecs issues it.
+    * 256x256 scene (seed 0): the latency of one launch (timed alone between
+      its own events after a 256 MiB write empties L2, median of 20) and the
+      mean launch time back to back (its 256 KiB input stays in L2)."""
+    sh = stream.cuda_stream
+    dev = stream.device
+    side = 4096
+    img = workloads.stress(side, side, 2)
+    n_out = g.out_size(side, side)
+    srcs = [torch.from_numpy(img.reshape(-1)).to(dev) for _ in range(4)]
+    outs = [torch.empty(n_out, dtype=torch.uint8, device=dev) for _ in range(4)]
+    n = max(args.steps, 40)
+    names = {g.CODEC_BC1: "bc1", g.CODEC_ETC1S: "etc1s"}
+    stress = {"workload": "4096x4096 stress quarters (seed 2: uniform noise, constant blocks, two-colour blocks, "
+                          "grey with random alpha)"}
+
+    def check(rc):
+        if rc != g.OK:
+            raise RuntimeError("stress: %s %s" % (g.status_string(rc), g.last_error()))
+
+    for c in codecs:
+        us = back_to_back_us(torch, stream, lambda k, c=c: check(
+            g.compress_device(c, outs[k % 4].data_ptr(), srcs[(k + 1) % 4].data_ptr(), side, side, 4 * side, sh)), n)
+        gbs = ALG_BYTES_PER_PX * side * side / us / 1e3
+        stress[names[c]] = {"mean_launch_us": round(us, 2), "mpix_s": round(side * side / us, 1),
+                            "hbm_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    pair_us = back_to_back_us(torch, stream, lambda k: check(
+        g.compress_device(codecs[k % 2], outs[k % 4].data_ptr(), srcs[(k + 1) % 4].data_ptr(), side, side, 4 * side,
+                          sh)), 2 * (n // 2)) * 2
+    stress["alternating_pair_us"] = round(pair_us, 2)
+    stress["timing"] = ("mean of %d launches back to back between two CUDA events (median of 3 rounds), input "
+                        "rotating over 4 device copies (256 MiB > L2), output over 4 buffers; alternating_pair_us = "
+                        "one BC1 launch + one ETC1s launch, alternating" % n)
+    del srcs, outs
+
+    side = 256
+    img = workloads.scene(side, side, 0)
+    src = torch.from_numpy(img.reshape(-1)).to(dev)
+    dst = [torch.empty(g.out_size(side, side), dtype=torch.uint8, device=dev) for _ in range(2)]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    small = {"workload": "256x256 scene (seed 0, stride 1024 B)"}
+    for c in codecs:
+        ts = []
+        for r in range(22):
+            flush.fill_(r & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = g.compress_device(c, dst[0].data_ptr(), src.data_ptr(), side, side, 4 * side, sh)
+            e1.record(stream)
+            check(rc)
+            e1.synchronize()
+            if r >= 2:
+                ts.append(e0.elapsed_time(e1) * 1e3)
+        b2b = back_to_back_us(torch, stream, lambda k, c=c: check(
+            g.compress_device(c, dst[k % 2].data_ptr(), src.data_ptr(), side, side, 4 * side, sh)), 200)
+        small[names[c]] = {"latency_us": round(statistics.median(ts), 2), "latency_min_us": round(min(ts), 2),
+                           "back_to_back_us": round(b2b, 2)}
+    small["timing"] = ("latency: one launch between its own two CUDA events after a 256 MiB write (L2 cold), median "
+                       "of 20; back_to_back: mean of 200 launches between two events (input L2-resident)")
+    del flush
+    return {"4096x4096": stress, "256x256": small}
 
 
 def run_pair(args, g, torch, src, dst, codecs, stream, device):
@@ -722,17 +809,14 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from goofy_gb300 import build as lib_build
-    from goofy_gb300 import workloads
+    # nothing of the GPU library is built or loaded on this arm: the scene comes
+    # from the generator compiled into the oracle library
+    import oracle
     from oracle import build as oracle_build
 
-    lib_build.build()
     oracle_build.build()
-    img = workloads.scene(W, H, SEED, PERIOD_SCALE, RECTS, threads=0)
-    import oracle
-
-    ref = oracle.load_ref()
-    fn, kind = (ref.ref_compress_mt, "reference") if ref is not None else (oracle.load().oracle_compress_mt, "port")
+    img = oracle.scene(W, H, SEED, PERIOD_SCALE, RECTS, threads=0)
+    fn, kind, label = oracle.ref_encoder()
     cores = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_encode_all(fn, img, cores)
@@ -744,11 +828,9 @@ def run_reference(args):
     line = {"metric": METRIC, "value": round(value, 1), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "pixels_per_step": 2 * W * H,
-                       "implementation": "reference encoder compiled from its sources" if kind == "reference"
-                       else "oracle port of the reference encoder (reference sources absent on this host)"},
+            "config": {"workload": WORKLOAD, "pixels_per_step": 2 * W * H, "implementation": label},
             "cpu_baseline": {"value": round(value, 1), "unit": "MPix/s", "cores": cores, "kind": kind,
-                             "cpu": "%s, %s" % (cpu_model(), platform.machine()),
+                             "implementation": label, "cpu": "%s, %s" % (cpu_model(), platform.machine()),
                              "sample": "full 8192x8192 image per step, BC1 + ETC1s, block rows striped over "
                                        "%d threads" % cores},
             "e2e": {"value": round(value, 1), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -811,10 +893,17 @@ def run_gpu(args):
                         ts.append(e0.elapsed_time(e1) * 1e3)
                     print("sweep %s threads=%d bpt=%d persistent=%d median_us=%.2f min_us=%.2f" % (
                         names[c], threads, bpt, pers, statistics.median(ts), min(ts)), file=sys.stderr)
+    # tuned tiles go to a cache file of this run (the library's per-user default is left alone)
+    import tempfile
+
+    cache_dir = tempfile.mkdtemp(prefix="goofy_tiles_")
+    g.set_tile_cache_path(os.path.join(cache_dir, "tiles.txt"))
     if not args.no_autotune:
-        for c in codecs:
-            tile, us = g.autotune(c, dst[c].data_ptr(), src[c].data_ptr(), W, H, 4 * W, reps=7)
-            tuned[names[c]] = {"tile": list(tile), "median_us": round(us, 2)}
+        # the step alternates the codecs, so the pair is tuned together (goofy_gpu_autotune_pair)
+        t_bc1, t_etc1s, us = g.autotune_pair(dst[0].data_ptr(), dst[1].data_ptr(), src[0].data_ptr(), W, H, 4 * W,
+                                             reps=7)
+        tuned = {"bc1": list(t_bc1), "etc1s": list(t_etc1s), "pair_us": round(us, 2),
+                 "api": "goofy_gpu_autotune_pair (alternating BC1 / ETC1s launches)"}
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -851,6 +940,29 @@ def run_gpu(args):
             per_launch[c] = e0.elapsed_time(e1) / args.steps
     total_ms = start.elapsed_time(end)
     total_ms = max_over_ranks(total_ms, world)
+
+    # the tile cache as a new process's first call sees it: defaults back, the
+    # tuned tiles read from the file again, the same K steps timed with them
+    tile_cache = None
+    if not args.no_autotune:
+        tuned_tiles = {names[c]: list(g.get_tile(c)) for c in codecs}
+        g.reset_tiles()
+        reloaded = g.load_tile_cache(local)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(3):
+            step()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cached_ms = e0.elapsed_time(e1) / args.steps
+        tile_cache = {"tiles_tuned": tuned_tiles, "tiles_after_reload": {names[c]: list(g.get_tile(c)) for c in codecs},
+                      "entries_installed": reloaded, "step_us_tuned": round(1e3 * total_ms / args.steps, 2),
+                      "step_us_cached": round(1e3 * cached_ms, 2),
+                      "cached_over_tuned": round(cached_ms / (total_ms / args.steps), 4),
+                      "note": "after goofy_gpu_reset_tiles + goofy_gpu_load_tile_cache, as the first call of a new "
+                              "process installs them (cache file of this run)"}
 
     px_per_step = 2 * W * H
     value = job_rate_mpix_s(world, px_per_step, args.steps, total_ms)
@@ -955,7 +1067,7 @@ def run_gpu(args):
     pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
     two_streams = run_two_streams(args, g, torch, src, dst, codecs, stream) if single else None
     both = run_both(args, g, torch, img, src, dst, codecs, stream) if single else None
-    cold = run_cold_configs(g, torch, workloads, codecs, stream) if single else None
+    small = run_small_configs(args, g, torch, workloads, codecs, stream, peak) if single else None
     batched = None
     if not args.no_batched and single:
         batched = run_batched(args, g, torch, stream, dev)
@@ -974,10 +1086,12 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
                        "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
                        "tiles": tiles, "autotune": tuned or None},
-            "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams, "both_codecs_one_pass": both, "cold_configs": cold, "batched": batched,
-            "serving": serving,
+            "serving": serving, "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams,
+            "both_codecs_one_pass": both, "small_configs": small, "batched": batched, "tile_cache": tile_cache,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
+    line["summary"] = summary(line, peak)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -87,20 +87,24 @@ def test_peak_is_the_measured_copy_bandwidth():
 
 
 class _FakeTensor:
+    count = [0]
+
     def __init__(self, n):
         self.n = n
+        _FakeTensor.count[0] += 1
+        self.ptr = 4096 * _FakeTensor.count[0]
 
     def fill_(self, v):
         return self
 
     def to(self, device):
-        return self
+        return _FakeTensor(self.n)
 
     def reshape(self, *a):
         return self
 
     def data_ptr(self):
-        return 4096
+        return self.ptr
 
 
 class _FakeEvent:
@@ -135,9 +139,10 @@ class _FakeTorch:
         return _FakeTensor(a.size)
 
 
-def test_cold_configs_bookkeeping():
-    """run_cold_configs: one flush and one bracketed launch per rep, two
-    untimed ones first, median / min / rates per codec and workload."""
+def test_small_configs_bookkeeping():
+    """run_small_configs: the stress image's launches run back to back between
+    two events with the input rotating over 4 copies and the output over 4
+    buffers; the 256x256 latency brackets each launch alone after a flush."""
     import types
 
     import numpy as np
@@ -151,8 +156,11 @@ def test_cold_configs_bookkeeping():
             return w * h // 2
 
         def compress_device(self, c, dst, src, w, h, stride, sh):
-            calls.append((c, w, h, stride))
+            calls.append((c, dst, src, w, stride))
             return 0
+
+        def status_string(self, rc):
+            return "?"
 
         def last_error(self):
             return ""
@@ -160,9 +168,30 @@ def test_cold_configs_bookkeeping():
     work = types.SimpleNamespace(scene=lambda w, h, s: np.zeros((h, 4 * w), np.uint8),
                                  stress=lambda w, h, s: np.zeros((h, 4 * w), np.uint8))
     stream = types.SimpleNamespace(cuda_stream=0, device="cuda:0")
-    res = bench.run_cold_configs(FakeLib(), _FakeTorch, work, (0, 1), stream, reps=4)
-    assert set(res) == {"256x256", "4096x4096", "timing"}
-    assert len(calls) == 2 * 2 * (4 + 2) and {(w, s) for _, w, _, s in calls} == {(256, 1024), (4096, 16384)}
+    args = types.SimpleNamespace(steps=10)
+    res = bench.run_small_configs(args, FakeLib(), _FakeTorch, work, (0, 1), stream, peak=6800.0)
+    n = 40  # max(steps, 40) launches a round
+    big = [c for c in calls if c[3] == 4096]
+    small = [c for c in calls if c[3] == 256]
+    assert len(big) == 2 * (2 + 3 * n) + (2 + 3 * n) and {s for *_, s in big} == {16384}
+    assert len({c[2] for c in big}) == 4 and len({c[1] for c in big}) == 4  # 4 inputs, 4 outputs
+    assert len(small) == 2 * (22 + 2 + 3 * 200) and {s for *_, s in small} == {1024}
     r = res["4096x4096"]["etc1s"]
-    assert r["median_us"] == r["min_us"] == 5.0  # every launch spans one 5 us tick of the fake clock
-    assert r["mpix_s"] == round(4096 * 4096 / 5.0, 1) and r["hbm_gbs"] == round(4.5 * 4096 * 4096 / 5.0 / 1e3, 1)
+    assert r["mean_launch_us"] == round(5.0 / n, 2)  # one 5 us tick of the fake clock over n launches
+    assert r["frac"] == round(4.5 * 4096 * 4096 / (5.0 / n) / 1e3 / 6800.0, 4)
+    assert res["256x256"]["bc1"]["latency_us"] == 5.0
+    assert res["4096x4096"]["alternating_pair_us"] == round(2 * 5.0 / n, 2)
+
+
+def test_summary_reads_the_sections_it_quotes():
+    line = {"ms_per_step": 0.1, "config": {"pixels_per_step": 2 * 8192 * 8192},
+            "per_codec": {"bc1": {"mean_launch_us": 43.0}, "etc1s": {"mean_launch_us": 46.0}},
+            "roofline": {"frac": 0.95}, "small_configs": {"4096x4096": {"bc1": {"mean_launch_us": 14.0,
+                                                                                 "frac": 0.8}}},
+            "serving": {"staged": {"loads": {"50%": {"p99_ms": 0.5, "by_class": {"probe_1024x1024":
+                                                                               {"p99_ms": 0.6}}}}}}}
+    s = bench.summary(line, 6800.0)
+    assert s["step_us"] == 100.0 and s["bc1_8192_us"] == 43.0 and s["stress4096_bc1_frac"] == 0.8
+    assert s["stress4096_etc1s_us"] is None and s["serve_staged_50pct_probe_p99_ms"] == 0.6
+    assert s["step_frac"] == round(4.5 * 2 * 8192 * 8192 / 1e-4 / 1e9 / 6800.0, 4)
+    assert len(json.dumps(s)) < 1000
