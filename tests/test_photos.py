@@ -108,3 +108,27 @@ def test_harness_files_byte_for_byte(built):
         got["parrot_red_simd_goofy_%s.%s" % (kind, ext)] = g.container(codec, [(blocks, w, h)])
         got["parrot_red_simd_goofy_%s_decompressed.tga" % kind] = g.tga(dec, w, h)
     assert {k: hashlib.sha256(v).hexdigest() for k, v in got.items()} == want
+
+
+def test_photo_fixtures_match_the_oracle(built):
+    """The committed photograph fixtures (tests/golden/photo_fixtures.npz, the
+    GPU photograph tests' inputs where the photographs are absent): the whole
+    photograph is the digested one, and the oracle gives the recorded
+    reference blocks and quality record of every fixture."""
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "photo_fixtures.npz"))
+    meta = json.loads(str(d["meta"]))
+    assert set(meta["fixtures"]) >= {"patterns", "kodim03_crop", "kodim23_crop", "parrot_red_crop"}
+    assert meta["fixtures"]["patterns"]["rgba_sha256"] == DIGESTS["photos"]["patterns"]["rgba_sha256"]
+    for codec in ("bc1", "etc1s"):
+        assert meta["fixtures"]["patterns"][codec]["sha256"] == DIGESTS["photos"]["patterns"][codec]["sha256"]
+    assert len(meta["harness_files_patterns"]) == 6
+    for name, f in meta["fixtures"].items():
+        img, w, h = d["rgba_" + name], f["width"], f["height"]
+        assert img.shape == (h, 4 * w) and _sha(img) == f["rgba_sha256"]
+        for codec, cname in enumerate(("bc1", "etc1s")):
+            out = oracle.encode(codec, img, w, h, any_width=False)
+            assert _sha(out) == f[cname]["sha256"], (name, cname)
+            dec, bad = oracle.decode(codec, out, w, h)
+            q = oracle.mse_psnr(img, dec, w, h)
+            for k, v in f[cname]["mse_psnr"].items():
+                assert q[k] == pytest.approx(v, rel=1e-12), (name, cname, k)
