@@ -205,8 +205,11 @@ GOOFY_FN uint2 encode_bc1(const uint32_t (&w)[16])
 // ---------------------------------------------------------------------------
 // ETC1s: returns {word0, word1} as the reference stores them (little-endian
 // u32s of the big-endian ETC1 block).  goofy_tc.h:1358-1493.
-// `ctrl_lut` holds etc_control_byte(2*i) for i < 128.
+// `ctrl_lut` holds etc_control_byte(2*i) for i < 128.  With FROM_BC1 the
+// index word is not computed here: word1 returns 0 and the caller derives it
+// from the BC1 indices of the block (etc1s_indices_from_bc1).
 // ---------------------------------------------------------------------------
+template <bool FROM_BC1 = false>
 GOOFY_FN uint2 etc1s_from_extents(const uint32_t (&w)[16], const BlockLanes& l, const Extents& e,
                                   const uint8_t* ctrl_lut)
 {
@@ -254,6 +257,7 @@ GOOFY_FN uint2 etc1s_from_extents(const uint32_t (&w)[16], const BlockLanes& l, 
     const uint32_t c_g = min(max(m_g + (uint32_t)d, 257u), 511u);
     const uint32_t rgb = c_rb + c_g * 256u - 257u * 0x00010101u;  // bytes 0, 1, 2: clamped R, G, B - 257
     const uint32_t word0 = (uint32_t)ctrl_lut[br.range >> 1] << 24 | (rgb & 0x00f8f8f8u);
+    if constexpr (FROM_BC1) return make_uint2(word0, 0u);
 
     // indices: bit j = not gez, bit 16+j = not lqt of the pixel with
     // j = 4*(x^2) + y (transposeAs4x4x4 order, goofy_tc.h:1366-1395).
@@ -287,6 +291,36 @@ GOOFY_FN uint2 etc1s_from_extents(const uint32_t (&w)[16], const BlockLanes& l, 
     return make_uint2(word0, word1);
 }
 
+// ETC1s word 1 from the BC1 index word of the same block.  Both codecs take
+// the same two tests per pixel from the same brightness statistics (gez:
+// Y >= mid; lqt: |Y - mid| < qt), so their index words hold the same 32 bits
+// in another order: BC1 keeps pixel i = 4y + x at bits 2i (not gez) and
+// 2i + 1 (lqt), ETC1s keeps not gez at bit j and not lqt at bit 16 + j, with
+// j = 4(x ^ 2) + y.  Fixed bit permutation, by delta swaps (each swaps the
+// bit pairs (p, p + s) selected by a mask):
+//  1. three rounds of the inverse perfect shuffle: byte 0 / 2 then hold the
+//     not-gez bits of pixels 0-7 / 8-15, byte 1 / 3 the lqt bits;
+//  2. the 4x4 transpose (y, x) -> (x, y) of both bit planes at once: 2x2
+//     blocks (pairs 3 apart), then the off-diagonal 2x2 blocks, which lie in
+//     different bytes here (pairs 14 apart);
+//  3. one byte permute for x -> x ^ 2 (pixels 0-7 and 8-15 trade places) and
+//     the order of the two halves; lqt inverted on the way in.
+GOOFY_FN uint32_t etc1s_indices_from_bc1(uint32_t idx)
+{
+    uint32_t x = idx ^ 0xaaaaaaaau, t;  // lqt -> not lqt
+    t = (x ^ (x >> 1)) & 0x22222222u;
+    x ^= t ^ (t << 1);
+    t = (x ^ (x >> 2)) & 0x0c0c0c0cu;
+    x ^= t ^ (t << 2);
+    t = (x ^ (x >> 4)) & 0x00f000f0u;
+    x ^= t ^ (t << 4);
+    t = (x ^ (x >> 3)) & 0x0a0a0a0au;
+    x ^= t ^ (t << 3);
+    t = (x ^ (x >> 14)) & 0x0000ccccu;
+    x ^= t ^ (t << 14);
+    return perm(x, 0u, 0x1302u);
+}
+
 GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
 {
     BlockLanes l;
@@ -295,15 +329,16 @@ GOOFY_FN uint2 encode_etc1s(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
 }
 
 // Both codecs from one set of lanes and extents: the R/B masks, the min / max
-// trees, the brightness statistics and the per-pixel luma sums are computed
-// once.  {BC1 block, ETC1s block}, each bit-identical to its own encoder's.
+// trees and the brightness statistics are computed once, and the ETC1s index
+// word is a bit permutation of the BC1 one.  {BC1 block, ETC1s block}, each
+// bit-identical to its own encoder's.
 GOOFY_FN uint4 encode_both(const uint32_t (&w)[16], const uint8_t* ctrl_lut)
 {
     BlockLanes l;
     block_lanes(w, l);
     const Extents e = lane_extents(l);
-    const uint2 a = bc1_from_extents(w, e), b = etc1s_from_extents(w, l, e, ctrl_lut);
-    return make_uint4(a.x, a.y, b.x, b.y);
+    const uint2 a = bc1_from_extents(w, e), b = etc1s_from_extents<true>(w, l, e, ctrl_lut);
+    return make_uint4(a.x, a.y, b.x, etc1s_indices_from_bc1(a.y));
 }
 
 template <int CODEC>
