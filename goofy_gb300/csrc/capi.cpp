@@ -736,19 +736,30 @@ GOOFY_EXPORT int goofy_gpu_autotune_pair(void* dst_bc1, void* dst_etc1s, const v
     uint8_t* out[2] = {static_cast<uint8_t*>(dst_bc1), static_cast<uint8_t*>(dst_etc1s)};
     Timer tm;
     if ((rc = tm.init()) != GOOFY_OK) return rc;
-    // each codec alone first; the pairs of each codec's kFinalists fastest shapes then run as the
-    // alternating BC1 / ETC1s sequence a caller encoding every image with both codecs issues
-    constexpr size_t kFinalists = 4;
+    // Each codec alone first.  Finalists per codec: its three fastest shapes and its three fastest
+    // bulk-copy shapes (a bulk-copy BC1 launch hands the SMs to a bulk-copy ETC1s launch without a
+    // gap, so it can win the pair while losing alone).  The finalists' pairs then run as the
+    // alternating BC1 / ETC1s launches on one image that a caller encoding every image with both
+    // codecs issues.
     std::vector<std::pair<float, Tile>> ranked[2];
-    for (int c = 0; c < 2; ++c)
+    std::vector<Tile> finalists[2];
+    for (int c = 0; c < 2; ++c) {
         if ((rc = rank_tiles(tm, c, out[c], nullptr, in, stride, width, height, access, reps, &ranked[c])) !=
             GOOFY_OK)
             return rc;
+        size_t fast = 0, bulk = 0;
+        for (const auto& r : ranked[c]) {
+            const bool is_bulk = r.second.persistent == 2;
+            if (fast < 3 || (is_bulk && bulk < 3)) finalists[c].push_back(r.second);
+            ++fast;
+            if (is_bulk) ++bulk;
+        }
+    }
     Tile best[2] = {ranked[0][0].second, ranked[1][0].second};
     float best_time = -1.f;
-    for (size_t i = 0; i < std::min(kFinalists, ranked[0].size()); ++i)
-        for (size_t j = 0; j < std::min(kFinalists, ranked[1].size()); ++j) {
-            const Tile t[2] = {ranked[0][i].second, ranked[1][j].second};
+    for (const Tile& t0 : finalists[0])
+        for (const Tile& t1 : finalists[1]) {
+            const Tile t[2] = {t0, t1};
             float ms = 0.f;
             const cudaError_t e = tm.time(reps, ms, [&](uint32_t k) -> cudaError_t {
                 cudaError_t r = goofy_gpu::launch_image(GOOFY_CODEC_BC1, in, stride, out[0], width, height, t[0],

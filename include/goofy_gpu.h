@@ -163,12 +163,13 @@ int goofy_gpu_autotune(int codec, void* dst, const void* src, uint32_t width, ui
 /* Autotuner for callers that encode every image with both codecs, one call
  * after the other (as the reference harness calls goofy::compressDXT1 and
  * goofy::compressETC1 on each image): ranks each codec's tiles alone as
- * goofy_gpu_autotune does, then times the alternating BC1 / ETC1s launches for
- * the pairs of each codec's four fastest tiles -- a shape that is fastest
- * alone can leave a gap where the other codec's launch takes over the SMs --
- * and installs the fastest pair.  best_us: the mean time of one BC1 + ETC1s
- * pair.  Both outputs (dst_bc1, dst_etc1s) must not overlap.  Synchronous.  No
- * reference counterpart. */
+ * goofy_gpu_autotune does, then times the alternating BC1 / ETC1s launches on
+ * the image for the pairs of each codec's finalists -- its three fastest
+ * tiles and its three fastest bulk-copy tiles (mode 2); a shape that is
+ * fastest alone can leave a gap where the other codec's launch takes over
+ * the SMs -- and installs the fastest pair.  best_us: the mean time of one
+ * BC1 + ETC1s pair.  Both outputs (dst_bc1, dst_etc1s) must not overlap.
+ * Synchronous.  No reference counterpart. */
 int goofy_gpu_autotune_pair(void* dst_bc1, void* dst_etc1s, const void* src, uint32_t width, uint32_t height,
                             uint32_t stride, uint32_t reps, goofy_gpu_tile* best_bc1, goofy_gpu_tile* best_etc1s,
                             float* best_us);

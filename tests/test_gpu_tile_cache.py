@@ -61,3 +61,29 @@ def test_autotune_records_its_pick(cache, cuda):
     assert g.tile_cache_lookup(cache, name, sms, g.CODEC_ETC1S) == tile
     cuda.cuda.synchronize()
     np.testing.assert_array_equal(dst.cpu().numpy(), oracle.encode(g.CODEC_ETC1S, img, w, h))
+
+
+def test_pair_autotune_installs_and_records_both(cache, cuda):
+    """goofy_gpu_autotune_pair: both codecs' tiles installed and recorded, and
+    the alternating launches with them stay bit-exact."""
+    name, sms = g.device_key(0)
+    w, h = 1024, 512
+    img = workloads.scene(w, h, 3)
+    src = cuda.from_numpy(img.reshape(-1)).cuda()
+    n = g.out_size(w, h)
+    dst = cuda.empty(2 * n, dtype=cuda.uint8, device="cuda")
+    t_bc1, t_etc1s, us = g.autotune_pair(dst.data_ptr(), dst.data_ptr() + n, src.data_ptr(), w, h, 4 * w, reps=2)
+    assert us > 0
+    assert g.get_tile(g.CODEC_BC1) == t_bc1 and g.get_tile(g.CODEC_ETC1S) == t_etc1s
+    assert g.tile_cache_lookup(cache, name, sms, g.CODEC_BC1) == t_bc1
+    assert g.tile_cache_lookup(cache, name, sms, g.CODEC_ETC1S) == t_etc1s
+    stream = cuda.cuda.current_stream().cuda_stream
+    out = cuda.zeros(2 * n, dtype=cuda.uint8, device="cuda")
+    for c in (g.CODEC_BC1, g.CODEC_ETC1S):
+        assert g.compress_device(c, out.data_ptr() + c * n, src.data_ptr(), w, h, 4 * w, stream) == g.OK
+    cuda.cuda.synchronize()
+    for c in (g.CODEC_BC1, g.CODEC_ETC1S):
+        np.testing.assert_array_equal(out[c * n:(c + 1) * n].cpu().numpy(), oracle.encode(c, img, w, h))
+    # overlapping outputs are refused
+    assert g.lib().goofy_gpu_autotune_pair(dst.data_ptr(), dst.data_ptr() + 8, src.data_ptr(), w, h, 4 * w, 2,
+                                           None, None, None) == g.ERR_INVALID
