@@ -49,6 +49,10 @@ SEED, PERIOD_SCALE, RECTS = 1, 32, 2048
 ALG_BYTES_PER_PX = 4.5
 WORKLOAD = ("plain BC1 + ETC1s encode of one 8192x8192 RGBA8 synthetic scene (stride 32768 B, seed 1, "
             "value-noise periods x32, 2048 rectangles)")
+# the same `config` on both arms (GPU and reference CPU)
+CONFIG = {"workload": WORKLOAD, "pixels_per_step": 2 * W * H,
+          "l2": "inputs larger than L2: 256 MiB per image (the GPU's L2 is 129 MB); the GPU arm alternates two "
+                "device copies of it between the codecs"}
 
 
 def parse():
@@ -69,7 +73,7 @@ def parse():
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     p.add_argument("--profile", choices=["encode", "quality", "mips", "batch", "batch-pipeline", "both"],
                    help="only run a few launches of one kernel family (for ncu captures) and exit")
-    p.add_argument("--profile-size", type=int, default=4096, help="image side for --profile")
+    p.add_argument("--profile-size", default="4096", help="image size for --profile: a side (square) or WxH")
     return p.parse_args()
 
 
@@ -188,6 +192,43 @@ class ClockSampler:
         return out
 
 
+def cpu_throttle_stats():
+    """CPU-quota throttling of this process's cgroup so far (cgroup v2
+    cpu.stat, else v1 cpu/cpu.stat): periods, throttled periods and
+    throttled microseconds; {} where the files are absent."""
+    for path, unit in (("/sys/fs/cgroup/cpu.stat", 1.0), ("/sys/fs/cgroup/cpu/cpu.stat", 1e-3),
+                       ("/sys/fs/cgroup/cpu,cpuacct/cpu.stat", 1e-3)):
+        try:
+            kv = dict(l.split() for l in open(path) if len(l.split()) == 2)
+        except OSError:
+            continue
+        us = kv.get("throttled_usec")
+        us = float(us) if us is not None else float(kv.get("throttled_time", 0)) * unit
+        return {"periods": int(kv.get("nr_periods", 0)), "throttled": int(kv.get("nr_throttled", 0)),
+                "throttled_us": us}
+    return {}
+
+
+def throttle_delta(a, b):
+    if not a or not b:
+        return None
+    return {k: round(b[k] - a[k], 1) for k in a}
+
+
+def cpu_quota():
+    """The cgroup's CPU quota as "quota period" (v2 cpu.max / v1 cfs files), or None."""
+    try:
+        return open("/sys/fs/cgroup/cpu.max").read().strip()
+    except OSError:
+        pass
+    try:
+        q = open("/sys/fs/cgroup/cpu/cpu.cfs_quota_us").read().strip()
+        p = open("/sys/fs/cgroup/cpu/cpu.cfs_period_us").read().strip()
+        return "%s %s" % (q, p)
+    except OSError:
+        return None
+
+
 def cpu_encode_all(lib_fn, img, threads, outs=None):
     """Both codecs over the whole image; returns seconds."""
     import numpy as np
@@ -293,7 +334,7 @@ def summary(line, peak):
            "step_frac": round(ALG_BYTES_PER_PX * line["config"]["pixels_per_step"] / (line["ms_per_step"] * 1e-3)
                               / 1e9 / peak, 4),
            "dominant_frac": get("roofline", "frac"),
-           "tiles": get("config", "tiles"), "cached_tiles_step_ratio": get("tile_cache", "cached_over_tuned"),
+           "tiles": get("tiles"), "cached_tiles_step_ratio": get("tile_cache", "cached_over_tuned"),
            "stress4096_bc1_us": get("small_configs", "4096x4096", "bc1", "mean_launch_us"),
            "stress4096_etc1s_us": get("small_configs", "4096x4096", "etc1s", "mean_launch_us"),
            "stress4096_bc1_frac": get("small_configs", "4096x4096", "bc1", "frac"),
@@ -734,7 +775,8 @@ def run_serving(args, g, device):
                           "probe, BC1/ETC1s 50/50, pinned host in/out, device budget 16 GiB",
               "offered_load_basis": "fraction of the server's own measured capacity (all requests arriving at "
                                     "once); every request crosses the host link, whose measured H2D ceiling "
-                                    "(~211 GB/s) caps serving far below the device-resident batched rate"}
+                                    "(~211 GB/s) caps serving far below the device-resident batched rate",
+              "host_cpus": os.cpu_count(), "cgroup_cpu_quota": cpu_quota()}
     try:
         for name, mode in (("staged", g.SERVER_STAGED), ("direct", g.SERVER_DIRECT)):
             srv = g.Server(mode=mode, device=device)
@@ -754,7 +796,9 @@ def run_serving(args, g, device):
                     rate = f * cap / float(px.mean())
                     n = max(200, int(rate * args.serve_seconds))
                     reqs, arrival, rpx, rprobe = stream(n, rate)
+                    thr0 = cpu_throttle_stats()
                     rc, lat, wall, stamps = srv.replay(reqs, arrival, with_times=True)
+                    thr1 = cpu_throttle_stats()
                     assert rc == g.OK, g.last_error()
                     loads["%d%%" % round(100 * f)] = {
                         "offered_mpix_s": round(f * cap / 1e6, 1), "requests": n,
@@ -763,7 +807,8 @@ def run_serving(args, g, device):
                         "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
                         "p999_ms": round(float(np.percentile(lat, 99.9)) / 1e6, 3),
                         "max_ms": round(float(lat.max()) / 1e6, 3),
-                        "by_class": classes(rpx, rprobe, lat), "p99_tail_phases_ms": tail_phases(lat, stamps)}
+                        "by_class": classes(rpx, rprobe, lat), "p99_tail_phases_ms": tail_phases(lat, stamps),
+                        "cpu_quota_throttling": throttle_delta(thr0, thr1)}
                 entry["loads"] = loads
                 entry["stats"] = srv.stats()
                 result[name] = entry
@@ -828,7 +873,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": round(value, 1), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "pixels_per_step": 2 * W * H, "implementation": label},
+            "config": dict(CONFIG), "implementation": label,
             "cpu_baseline": {"value": round(value, 1), "unit": "MPix/s", "cores": cores, "kind": kind,
                              "implementation": label, "cpu": "%s, %s" % (cpu_model(), platform.machine()),
                              "sample": "full 8192x8192 image per step, BC1 + ETC1s, block rows striped over "
@@ -1083,9 +1128,7 @@ def run_gpu(args):
     line = {"metric": METRIC, "value": round(value, 1), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "pixels_per_step": px_per_step, "per_gpu": "same workload on every GPU",
-                       "l2": "inputs larger than L2: two 256 MiB device copies alternate between the codecs",
-                       "tiles": tiles, "autotune": tuned or None},
+            "config": dict(CONFIG), "per_gpu": "same workload on every GPU", "tiles": tiles, "autotune": tuned or None,
             "serving": serving, "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams,
             "both_codecs_one_pass": both, "small_configs": small, "batched": batched, "tile_cache": tile_cache,
@@ -1100,7 +1143,7 @@ def run_gpu(args):
 
 
 def run_profile(args):
-    """A few launches of one kernel family on a --profile-size square scene,
+    """A few launches of one kernel family on a --profile-size scene,
     default tiles, nothing timed: the workload of the ncu captures under
     profiles/ (small enough for a full capture to end in a minute)."""
     import numpy as np
@@ -1152,33 +1195,35 @@ def run_profile(args):
             b.close()
         print(json.dumps({"profile": "batch", "textures": args.batch_textures, "levels": len(descs)}))
         return 0
-    n = args.profile_size
-    img = workloads.scene(n, n, SEED, n // 256, max(8, n * n // 32768), threads=0)
+    w, _, h = args.profile_size.partition("x")
+    w = int(w)
+    h = int(h) if h else w
+    img = workloads.scene(w, h, SEED, w // 256, max(8, w * h // 32768), threads=0)
     src = torch.from_numpy(img.reshape(-1)).cuda()
     sh = torch.cuda.current_stream().cuda_stream
-    dst = [torch.empty(g.out_size(n, n), dtype=torch.uint8, device="cuda") for _ in range(2)]
+    dst = [torch.empty(g.out_size(w, h), dtype=torch.uint8, device="cuda") for _ in range(2)]
     for c in (g.CODEC_BC1, g.CODEC_ETC1S):
         for _ in range(3 if args.profile == "encode" else 1):
-            assert g.compress_device(c, dst[c].data_ptr(), src.data_ptr(), n, n, 4 * n, sh) == g.OK, g.last_error()
+            assert g.compress_device(c, dst[c].data_ptr(), src.data_ptr(), w, h, 4 * w, sh) == g.OK, g.last_error()
     if args.profile == "both":
         for _ in range(3):
-            assert g.compress_both_device(dst[0], dst[1], src, n, n, 4 * n, sh) == g.OK, g.last_error()
+            assert g.compress_both_device(dst[0], dst[1], src, w, h, 4 * w, sh) == g.OK, g.last_error()
     if args.profile == "quality":
         sums = torch.zeros(6, dtype=torch.int64, device="cuda")
-        rgba = torch.empty(n * n * 4, dtype=torch.uint8, device="cuda")
+        rgba = torch.empty(w * h * 4, dtype=torch.uint8, device="cuda")
         bad = torch.zeros(1, dtype=torch.int64, device="cuda")
         for c in (g.CODEC_BC1, g.CODEC_ETC1S):
             for _ in range(3):
-                assert g.block_error_device(c, dst[c], src, n, n, 4 * n, sums, sh) == g.OK, g.last_error()
-            assert g.decode_device(c, rgba, 4 * n, dst[c], n, n, bad, sh) == g.OK, g.last_error()
+                assert g.block_error_device(c, dst[c], src, w, h, 4 * w, sums, sh) == g.OK, g.last_error()
+            assert g.decode_device(c, rgba, 4 * w, dst[c], w, h, bad, sh) == g.OK, g.last_error()
     if args.profile == "mips":
-        nbytes = g.lib().goofy_gpu_mip_arena_bytes(n, n)
+        nbytes = g.lib().goofy_gpu_mip_arena_bytes(w, h)
         arena = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
         base = arena.data_ptr() + (-arena.data_ptr()) % 256
         for _ in range(3):
-            g.generate_mips(src, n, n, 4 * n, base, nbytes, sh)
+            g.generate_mips(src, w, h, 4 * w, base, nbytes, sh)
     torch.cuda.synchronize()
-    print(json.dumps({"profile": args.profile, "size": n, "pipeline_timeouts": g.pipeline_timeouts()}))
+    print(json.dumps({"profile": args.profile, "size": [w, h], "pipeline_timeouts": g.pipeline_timeouts()}))
     return 0
 
 
