@@ -342,6 +342,7 @@ def summary(line, peak):
            "scene256_latency_us": [get("small_configs", "256x256", c, "latency_us") for c in ("bc1", "etc1s")],
            "both_one_pass_us": get("both_codecs_one_pass", "mean_launch_us"),
            "batched_speedup_vs_plain": get("batched", "speedup_vs_plain"),
+           "batch_16x2048_us": get("batch_16x2048", "mean_call_us"), "batch_16x2048_frac": get("batch_16x2048", "frac"),
            "batched_mpix_s": get("batched", "batched_mpix_s"),
            "e2e_mpix_s": get("e2e", "value"),
            "cpu_mpix_s": get("cpu_baseline", "value"), "cpu_kind": get("cpu_baseline", "kind")}
@@ -442,6 +443,33 @@ def run_small_configs(args, g, torch, workloads, codecs, stream, peak):
                        "of 20; back_to_back: mean of 200 launches between two events (input L2-resident)")
     del flush
     return {"4096x4096": stress, "256x256": small}
+
+
+def run_batch_16x2048(args, g, torch, workloads, stream, device):
+    """16 textures of 2048x2048 (8 BC1, 8 ETC1s; 256 MiB of input, twice the
+    L2) in one call of the pipelined batch kernel, its descriptors passed as
+    the kernel's parameter: mean of launches back to back between two
+    events, outputs alternating between two sets."""
+    side, n = 2048, 16
+    img = workloads.scene(side, side, 3, threads=0)
+    srcs = [torch.from_numpy(img.reshape(-1)).to(stream.device) for _ in range(n)]
+    outs = [[torch.empty(g.out_size(side, side), dtype=torch.uint8, device=stream.device) for _ in range(n)]
+            for _ in range(2)]
+    arrs = [g.images_array([(srcs[i].data_ptr(), outs[k][i].data_ptr(), side, side, 4 * side, i % 2)
+                            for i in range(n)]) for k in range(2)]
+    b = g.Batch(n, device)
+    try:
+        assert b.set_tile(512, 2, 1024, 1) == g.OK
+        sh = stream.cuda_stream
+        us = back_to_back_us(torch, stream, lambda k: b.encode(arrs[k % 2], sh), max(args.steps, 20))
+        same = all(bool(torch.equal(outs[0][i], outs[1][i])) for i in range(n))
+    finally:
+        b.close()
+    px = n * side * side
+    gbs = ALG_BYTES_PER_PX * px / us / 1e3
+    return {"workload": "16 textures of 2048x2048 (8 BC1, 8 ETC1s), one goofy_gpu_batch_encode call each",
+            "tile": [512, 2, 1024, 1], "mean_call_us": round(us, 2), "mpix_s": round(px / us, 1),
+            "hbm_gbs": round(gbs, 1), "frac": round(gbs / read_peaks()[0], 4), "outputs_equal_across_calls": same}
 
 
 def run_pair(args, g, torch, src, dst, codecs, stream, device):
@@ -1110,6 +1138,7 @@ def run_gpu(args):
     single = world == 1
     mips = run_mips(g, torch, workloads, img, src[0], stream) if single else None
     pair = run_pair(args, g, torch, src, dst, codecs, stream, local) if single else None
+    batch16 = run_batch_16x2048(args, g, torch, workloads, stream, local) if single else None
     two_streams = run_two_streams(args, g, torch, src, dst, codecs, stream) if single else None
     both = run_both(args, g, torch, img, src, dst, codecs, stream) if single else None
     small = run_small_configs(args, g, torch, workloads, codecs, stream, peak) if single else None
@@ -1131,7 +1160,7 @@ def run_gpu(args):
             "config": dict(CONFIG), "per_gpu": "same workload on every GPU", "tiles": tiles, "autotune": tuned or None,
             "serving": serving, "per_codec": per_codec, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "quality": quality, "mips": mips, "pair_batched": pair, "two_streams": two_streams,
-            "both_codecs_one_pass": both, "small_configs": small, "batched": batched, "tile_cache": tile_cache,
+            "both_codecs_one_pass": both, "small_configs": small, "batch_16x2048": batch16, "batched": batched, "tile_cache": tile_cache,
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
     line["summary"] = summary(line, peak)

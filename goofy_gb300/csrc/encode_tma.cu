@@ -231,10 +231,14 @@ constexpr size_t batch_tma_smem_bytes(const TmaLayout& l)
     return (size_t)l.stages * (l.stage_bytes + 16u + sizeof(UnitRec)) + 128u;
 }
 
-template <int BPT, int COMPUTE>
+// PARAM_TABLES: the descriptor and first-unit tables are the kernel's
+// parameter (readable before the dependency wait); otherwise they are device
+// memory the stream wrote before this launch.
+template <int BPT, int COMPUTE, bool PARAM_TABLES>
 __device__ __forceinline__ void batch_tma_body(const BatchImage* __restrict__ images, uint32_t n_images,
                                                const uint32_t* __restrict__ first_unit, uint32_t total_units)
 {
+    pdl_launch_dependents();
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t abort_flag;
     constexpr uint32_t compute_warps = COMPUTE / 32;
@@ -255,6 +259,31 @@ __device__ __forceinline__ void batch_tma_body(const BatchImage* __restrict__ im
     }
     fill_ctrl_lut(ctrl_lut);
     __syncthreads();
+    if constexpr (PARAM_TABLES) {
+        if (warp == compute_warps && lane == 0) {
+            // While the previous kernel in the stream drains, ask L2 for the rows
+            // of this CTA's first units (a hint, as in encode_image_tma: nothing
+            // enters the CTA and nothing is written before pdl_wait()).
+            uint32_t ii = 0;
+            for (uint32_t u = blockIdx.x, k = 0; u < total_units && k < L.stages; u += gridDim.x, ++k) {
+                ii += find_image(first_unit + ii, n_images - ii, u);
+                const BatchImage& im = images[ii];
+                if (!im.vec16 || im.bw * 8u < L.tile_blocks) continue;  // units the compute warps load themselves
+                const uint32_t first = (u - im.first_unit) * L.tile_blocks;
+                const uint32_t n = min(L.tile_blocks, im.bw * im.bh - first);
+                for (uint32_t gb = first; gb < first + n;) {
+                    uint32_t bx;
+                    const uint32_t by = div_magic(gb, im.bw, im.bw_magic, bx);
+                    const uint32_t nb = min(im.bw - bx, first + n - gb);
+                    const uint8_t* row = im.src + (size_t)by * 4u * im.stride + 16u * (size_t)bx;
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr) bulk_prefetch_l2(row + (size_t)rr * im.stride, 16u * nb);
+                    gb += nb;
+                }
+            }
+        }
+    }
+    pdl_wait();  // no copy and no store before the previous kernel in the stream is done
 
     if (warp == compute_warps) {  // producer
         if (lane != 0) return;
@@ -384,7 +413,7 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     encode_batch_tma(const BatchImage* __restrict__ images, uint32_t n_images, const uint32_t* __restrict__ first_unit,
                      uint32_t total_units)
 {
-    batch_tma_body<BPT, COMPUTE>(images, n_images, first_unit, total_units);
+    batch_tma_body<BPT, COMPUTE, false>(images, n_images, first_unit, total_units);
 }
 
 // The same tables in the kernel's parameter space (small batches).
@@ -392,7 +421,7 @@ template <int BPT, int COMPUTE>
 __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     encode_batch_tma_inline(const __grid_constant__ InlineBatch batch, uint32_t n_images, uint32_t total_units)
 {
-    batch_tma_body<BPT, COMPUTE>(batch.images, n_images, batch.first_unit, total_units);
+    batch_tma_body<BPT, COMPUTE, true>(batch.images, n_images, batch.first_unit, total_units);
 }
 
 namespace {
@@ -506,9 +535,8 @@ cudaError_t launch_batch_tma_t(const BatchImage* images, uint32_t n_images, cons
     if (resident == 0) return cudaErrorInvalidValue;
     if (ctas > (uint32_t)resident) ctas = (uint32_t)resident;
     constexpr size_t smem = batch_tma_smem_bytes(tma_layout(COMPUTE, BPT));
-    encode_batch_tma<BPT, COMPUTE><<<ctas ? ctas : 1u, COMPUTE + 32, smem, stream>>>(images, n_images, first_unit,
-                                                                                      total_units);
-    return cudaGetLastError();
+    return launch_pdl(encode_batch_tma<BPT, COMPUTE>, dim3(ctas ? ctas : 1u), dim3(COMPUTE + 32), smem, stream,
+                      images, n_images, first_unit, total_units);
 }
 
 template <int BPT, int COMPUTE>
@@ -532,9 +560,8 @@ cudaError_t launch_batch_tma_inline_t(const InlineBatch& batch, uint32_t n_image
         ready[dev].store(true, std::memory_order_relaxed);
     }
     if (ctas > (uint32_t)resident) ctas = (uint32_t)resident;
-    encode_batch_tma_inline<BPT, COMPUTE><<<ctas ? ctas : 1u, COMPUTE + 32, smem, stream>>>(batch, n_images,
-                                                                                             total_units);
-    return cudaGetLastError();
+    return launch_pdl(encode_batch_tma_inline<BPT, COMPUTE>, dim3(ctas ? ctas : 1u), dim3(COMPUTE + 32), smem,
+                      stream, batch, n_images, total_units);
 }
 
 }  // namespace

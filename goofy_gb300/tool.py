@@ -13,6 +13,11 @@
       images (decoded on the GPU) and the original and baseline images as
       TGA.
 
+  python -m goofy_gb300.tool autotune [--size N] [--cache PATH]
+      Tunes the image-kernel tiles on this GPU (both codecs together, then
+      the two-codec pass) on a synthetic NxN scene and records them in the
+      tile cache, which later processes' first calls install.
+
   python -m goofy_gb300.tool encode IN.png OUT.dds|OUT.ktx [--codec bc1|etc1s] [--mips] [--both]
       One PNG to a DDS (BC1) or KTX (ETC1s) file, optionally with a full mip
       chain generated on the GPU (power-of-two sizes) and all levels encoded
@@ -214,6 +219,35 @@ def _encode_both(args, levels, stream, torch):
     return 0
 
 
+def cmd_autotune(args):
+    """Tune the tiles on a synthetic scene of the given size and record them
+    in the tile cache (goofy_gpu_autotune_pair for BC1 and ETC1s, then
+    goofy_gpu_autotune for the two-codec pass)."""
+    import torch
+
+    from . import workloads
+
+    if args.cache is not None:
+        g.set_tile_cache_path(args.cache)
+    if not g.tile_cache_path():
+        raise SystemExit("the tile cache is disabled (GOOFY_TILE_CACHE is empty); give --cache PATH")
+    assert g.init(args.device) == g.OK, g.last_error()
+    torch.cuda.set_device(args.device)
+    w = h = args.size
+    img = workloads.scene(w, h, 1, max(1, w // 256), max(8, w * h // 32768), threads=0)
+    src = torch.from_numpy(img.reshape(-1)).cuda()
+    n = g.out_size(w, h)
+    out = torch.empty(2 * n, dtype=torch.uint8, device="cuda")
+    t_bc1, t_etc1s, us = g.autotune_pair(out.data_ptr(), out.data_ptr() + n, src.data_ptr(), w, h, 4 * w,
+                                         reps=args.reps)
+    t_both, us_both = g.autotune(g.CODEC_BOTH, out.data_ptr(), src.data_ptr(), w, h, 4 * w, reps=args.reps)
+    name, sms = g.device_key(args.device)
+    print("%s (%d SMs), %dx%d scene: bc1 %s + etc1s %s, %.2f us a pair; both-codec pass %s, %.2f us" %
+          (name, sms, w, h, t_bc1, t_etc1s, us, t_both, us_both))
+    print("recorded in", g.tile_cache_path())
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m goofy_gb300.tool", description=__doc__.split("\n")[0])
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -228,8 +262,13 @@ def main(argv=None):
     e.add_argument("--codec", choices=("bc1", "etc1s"))
     e.add_argument("--mips", action="store_true", help="add a GPU-generated mip chain")
     e.add_argument("--both", action="store_true", help="write OUT.dds and OUT.ktx from one pass over each level")
+    t = sub.add_parser("autotune", help="tune the kernel tiles for this GPU and record them in the tile cache")
+    t.add_argument("--size", type=int, default=8192, help="side of the synthetic scene to tune on")
+    t.add_argument("--reps", type=int, default=7, help="launches per timed round")
+    t.add_argument("--device", type=int, default=0)
+    t.add_argument("--cache", help="tile cache file (default: $GOOFY_TILE_CACHE or the per-user cache)")
     args = ap.parse_args(argv)
-    return cmd_run(args) if args.cmd == "run" else cmd_encode(args)
+    return {"run": cmd_run, "encode": cmd_encode, "autotune": cmd_autotune}[args.cmd](args)
 
 
 if __name__ == "__main__":

@@ -37,7 +37,7 @@ def test_roofline_traffic_comes_from_the_committed_profiles():
     profiles/, and they are close to the algorithmic 4.5 B/px of a launch
     (less where L2 still holds part of the output at the end)."""
     algorithmic = 4.5 * 8192 * 8192
-    for key in ("encode_image_kernel_bc1_8192", "encode_image_tma_etc1s_8192"):
+    for key in ("encode_image_tma_bc1_8192", "encode_image_tma_etc1s_8192"):
         t = bench.read_traffic(key)
         assert t is not None, key
         assert 0.9 * algorithmic < t <= 1.02 * algorithmic, (key, t)

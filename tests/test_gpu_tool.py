@@ -71,3 +71,24 @@ def test_run_prints_harness_rows(cuda, tmp_path):
     assert sorted(p.name for p in (tmp_path / "out").iterdir()) == [
         "a_baseline.tga", "a_gb300_goofy_dxt1.dds", "a_gb300_goofy_dxt1_decompressed.tga", "a_gb300_goofy_etc1.ktx",
         "a_gb300_goofy_etc1_decompressed.tga", "a_original.tga"]
+
+
+def test_autotune_records_the_tiles(cuda, tmp_path):
+    """`tool autotune` tunes on a small scene and writes this GPU model's
+    entries (both codecs and the two-codec pass) into the given cache file."""
+    import contextlib
+    import io
+
+    from goofy_gb300 import tool
+
+    cache = str(tmp_path / "tiles.txt")
+    try:
+        with contextlib.redirect_stdout(io.StringIO()) as out:
+            assert tool.main(["autotune", "--size", "512", "--reps", "1", "--cache", cache]) == 0
+        name, sms = g.device_key(0)
+        for c in (g.CODEC_BC1, g.CODEC_ETC1S, g.CODEC_BOTH):
+            assert g.tile_cache_lookup(cache, name, sms, c) == g.get_tile(c)
+        assert cache in out.getvalue()
+    finally:
+        g.reset_tiles()
+        g.set_tile_cache_path(None)
