@@ -69,6 +69,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=4.0, help="length of each offered-load run")
+    p.add_argument("--serve-soak-s", type=float, default=30.0, help="length of the staged server's 10%% load soak "
+                                                                     "window (0: none)")
     p.add_argument("--batch-textures", type=int, default=1000)
     p.add_argument("--sweep", action="store_true", help="print every tile shape's launch time to stderr")
     p.add_argument("--profile", choices=["encode", "quality", "mips", "batch", "batch-pipeline", "both"],
@@ -207,6 +209,30 @@ def cpu_throttle_stats():
         return {"periods": int(kv.get("nr_periods", 0)), "throttled": int(kv.get("nr_throttled", 0)),
                 "throttled_us": us}
     return {}
+
+
+def pressure_totals():
+    """Host pressure stall information (/proc/pressure): microseconds in
+    which some task waited for CPU, memory or IO, so far; {} if absent."""
+    out = {}
+    for res in ("cpu", "memory", "io"):
+        try:
+            for line in open("/proc/pressure/" + res):
+                if line.startswith("some"):
+                    out[res] = int(line.split("total=")[1])
+        except (OSError, IndexError, ValueError):
+            pass
+    return out
+
+
+def window_diagnostics(thr0, psi0, thr1, psi1, st):
+    """Per serving window: CPU-quota throttling, host pressure stall time and
+    the slowest launch's parts (server stats read and reset around the window)."""
+    return {"cpu_quota_throttling": throttle_delta(thr0, thr1),
+            "host_pressure_stall_ms": {k: round((psi1[k] - psi0[k]) / 1e3, 3) for k in psi1 if k in psi0},
+            "slowest_launch_ms": {"enqueue": round(st["max_enqueue_ns"] / 1e6, 3),
+                                  "kernel": round(st["max_kernel_ns"] / 1e6, 3),
+                                  "enqueue_to_done": round(st["max_launch_ns"] / 1e6, 3)}}
 
 
 def throttle_delta(a, b):
@@ -353,6 +379,7 @@ def summary(line, peak):
             out["serve_%s_50pct_probe_p99_ms" % mode] = get("serving", mode, "loads", "50%", "by_class",
                                                             "probe_1024x1024", "p99_ms")
     out["serve_vs_plain"] = get("serving", "plain", "server_vs_plain")
+    out["serve_staged_soak_10pct_max_ms"] = get("serving", "staged", "soak_10pct", "max_ms")
     return out
 
 
@@ -824,9 +851,10 @@ def run_serving(args, g, device):
                     rate = f * cap / float(px.mean())
                     n = max(200, int(rate * args.serve_seconds))
                     reqs, arrival, rpx, rprobe = stream(n, rate)
-                    thr0 = cpu_throttle_stats()
+                    thr0, psi0 = cpu_throttle_stats(), pressure_totals()
+                    srv.stats()  # resets the slowest-launch figures
                     rc, lat, wall, stamps = srv.replay(reqs, arrival, with_times=True)
-                    thr1 = cpu_throttle_stats()
+                    thr1, psi1, st = cpu_throttle_stats(), pressure_totals(), srv.stats()
                     assert rc == g.OK, g.last_error()
                     loads["%d%%" % round(100 * f)] = {
                         "offered_mpix_s": round(f * cap / 1e6, 1), "requests": n,
@@ -836,8 +864,24 @@ def run_serving(args, g, device):
                         "p999_ms": round(float(np.percentile(lat, 99.9)) / 1e6, 3),
                         "max_ms": round(float(lat.max()) / 1e6, 3),
                         "by_class": classes(rpx, rprobe, lat), "p99_tail_phases_ms": tail_phases(lat, stamps),
-                        "cpu_quota_throttling": throttle_delta(thr0, thr1)}
+                        **window_diagnostics(thr0, psi0, thr1, psi1, st)}
                 entry["loads"] = loads
+                if mode == g.SERVER_STAGED and args.serve_soak_s > 0:
+                    # one long low-load window: the rare stalls show in its max
+                    rate = 0.10 * cap / float(px.mean())
+                    reqs, arrival, rpx, _ = stream(max(200, int(rate * args.serve_soak_s)), rate)
+                    thr0, psi0 = cpu_throttle_stats(), pressure_totals()
+                    srv.stats()
+                    rc, lat, wall = srv.replay(reqs, arrival)
+                    thr1, psi1, st = cpu_throttle_stats(), pressure_totals(), srv.stats()
+                    assert rc == g.OK, g.last_error()
+                    entry["soak_10pct"] = {
+                        "seconds": args.serve_soak_s, "requests": len(reqs),
+                        "p50_ms": round(float(np.percentile(lat, 50)) / 1e6, 3),
+                        "p99_ms": round(float(np.percentile(lat, 99)) / 1e6, 3),
+                        "p999_ms": round(float(np.percentile(lat, 99.9)) / 1e6, 3),
+                        "max_ms": round(float(lat.max()) / 1e6, 3), "over_3ms": int((lat > 3e6).sum()),
+                        **window_diagnostics(thr0, psi0, thr1, psi1, st)}
                 entry["stats"] = srv.stats()
                 result[name] = entry
             finally:

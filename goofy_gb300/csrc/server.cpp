@@ -134,6 +134,8 @@ struct LaunchSlot {
     unsigned long long* d_qsums = nullptr;  // quality: 6 error sums per request
     unsigned long long* h_qsums = nullptr;
     cudaEvent_t ev_in = nullptr, ev_kernel = nullptr;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // timing events around the batch kernel
+    int64_t t_enqueue = 0;                         // start of this launch's enqueue (host clock)
     std::vector<uint64_t> tickets;
     bool busy = false;
 };
@@ -166,6 +168,7 @@ struct goofy_gpu_server {
 
     // stats
     uint64_t n_launches = 0, n_requests_done = 0, max_batch = 0, pixels_done = 0;
+    uint64_t max_enqueue_ns = 0, max_kernel_ns = 0, max_launch_ns = 0;  // since the last stats read
     int error = GOOFY_OK;
 
     Request& rec(uint64_t t) { return pool[t % pool.size()]; }
@@ -180,7 +183,9 @@ void CUDART_CB on_launch_done(void* p)
     const int64_t t = now_ns();
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        for (uint64_t tk : s->slots[a->slot].tickets) s->rec(tk).t_done = t;
+        LaunchSlot& sl = s->slots[a->slot];
+        for (uint64_t tk : sl.tickets) s->rec(tk).t_done = t;
+        s->max_launch_ns = std::max<uint64_t>(s->max_launch_ns, (uint64_t)(t - sl.t_enqueue));
         s->finished_slots.push_back(a->slot);
     }
     s->cv_sched.notify_one();
@@ -191,6 +196,11 @@ void retire_locked(goofy_gpu_server* s)
 {
     for (int si : s->finished_slots) {
         LaunchSlot& sl = s->slots[si];
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, sl.ev_k0, sl.ev_k1) == cudaSuccess)
+            s->max_kernel_ns = std::max<uint64_t>(s->max_kernel_ns, (uint64_t)(ms * 1e6f));
+        else
+            cudaGetLastError();
         for (size_t i = 0; i < sl.tickets.size(); ++i) {
             Request& r = s->rec(sl.tickets[i]);
             if (s->cfg.quality) {
@@ -249,6 +259,7 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
     uint64_t units = 0;
     const uint32_t n = (uint32_t)tickets.size();
     const int64_t t = now_ns();
+    sl.t_enqueue = t;
     for (uint32_t i = 0; i < n; ++i) {
         Request& r = s->rec(tickets[i]);
         r.t_launch = t;
@@ -290,8 +301,10 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
     GOOFY_CUDA_TRY(cudaMemsetAsync(sl.d_counter, 0, sizeof(uint32_t), s->s_compute));
     const uint32_t ctas = (uint32_t)std::min<uint64_t>((uint64_t)s->resident_ctas,
                                                        (units * 32 + s->tile.threads - 1) / s->tile.threads);
+    GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_k0, s->s_compute));
     GOOFY_CUDA_TRY(goofy_gpu::launch_batch(sl.d_desc, n, sl.d_first, (uint32_t)units, sl.d_counter, s->tile,
                                            ctas ? ctas : 1, s->s_compute));
+    GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_k1, s->s_compute));
     if (s->cfg.quality) {  // decode the fresh blocks and compare with each request's source, same units
         GOOFY_CUDA_TRY(cudaMemsetAsync(sl.d_qsums, 0, 6 * sizeof(unsigned long long) * n, s->s_compute));
         GOOFY_CUDA_TRY(cudaMemsetAsync(sl.d_counter, 0, sizeof(uint32_t), s->s_compute));
@@ -313,6 +326,9 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
         last = s->s_back;
     }
     GOOFY_CUDA_TRY(cudaLaunchHostFunc(last, on_launch_done, cb));
+    const uint64_t enq = (uint64_t)(now_ns() - t);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->max_enqueue_ns = std::max(s->max_enqueue_ns, enq);
     return GOOFY_OK;
 }
 
@@ -399,6 +415,8 @@ int init_server(goofy_gpu_server* s)
         }
         GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_in, cudaEventDisableTiming));
         GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_kernel, cudaEventDisableTiming));
+        GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k0));
+        GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k1));
     }
     s->resident_ctas = goofy_gpu::batch_resident_ctas(s->tile.threads, s->tile.bpt);
     s->pool.resize(c.max_requests);
@@ -420,6 +438,8 @@ void teardown(goofy_gpu_server* s)
         if (sl.h_qsums) cudaFreeHost(sl.h_qsums);
         if (sl.ev_in) cudaEventDestroy(sl.ev_in);
         if (sl.ev_kernel) cudaEventDestroy(sl.ev_kernel);
+        if (sl.ev_k0) cudaEventDestroy(sl.ev_k0);
+        if (sl.ev_k1) cudaEventDestroy(sl.ev_k1);
     }
     if (s->arena_mem) cudaFree(s->arena_mem);
     for (cudaStream_t st : {s->s_copy, s->s_compute, s->s_back})
@@ -560,6 +580,10 @@ GOOFY_EXPORT int goofy_gpu_server_get_stats(goofy_gpu_server* s, goofy_gpu_serve
     st->max_batch = s->max_batch;
     st->waiting = s->waiting.size();
     st->inflight_bytes = s->inflight_bytes;
+    st->max_enqueue_ns = s->max_enqueue_ns;
+    st->max_kernel_ns = s->max_kernel_ns;
+    st->max_launch_ns = s->max_launch_ns;
+    s->max_enqueue_ns = s->max_kernel_ns = s->max_launch_ns = 0;
     return GOOFY_OK;
 }
 

@@ -414,6 +414,13 @@ typedef struct goofy_gpu_request_times {
 
 typedef struct goofy_gpu_server_stats {
     uint64_t launches, requests_done, pixels_done, max_batch, waiting, inflight_bytes;
+    /* Slowest launch since the previous goofy_gpu_server_get_stats call, to
+     * tell where a late request lost its time: the scheduler thread's time
+     * in the CUDA calls that enqueue one launch (copies, kernels, callback),
+     * the GPU time of one launch's batch kernel (CUDA events around it), and
+     * the time from the start of its enqueue to its completion callback.
+     * Read and reset by each call. */
+    uint64_t max_enqueue_ns, max_kernel_ns, max_launch_ns;
 } goofy_gpu_server_stats;
 
 /* Defaults: device 0, staged, 16 GiB budget, 1024 requests per launch, 4
