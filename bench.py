@@ -230,9 +230,13 @@ def window_diagnostics(thr0, psi0, thr1, psi1, st):
     the slowest launch's parts (server stats read and reset around the window)."""
     return {"cpu_quota_throttling": throttle_delta(thr0, thr1),
             "host_pressure_stall_ms": {k: round((psi1[k] - psi0[k]) / 1e3, 3) for k in psi1 if k in psi0},
-            "slowest_launch_ms": {"enqueue": round(st["max_enqueue_ns"] / 1e6, 3),
-                                  "kernel": round(st["max_kernel_ns"] / 1e6, 3),
-                                  "enqueue_to_done": round(st["max_launch_ns"] / 1e6, 3)}}
+            "launch_max_ms": {"enqueue": round(st["max_enqueue_ns"] / 1e6, 3),
+                              "kernel": round(st["max_kernel_ns"] / 1e6, 3),
+                              "enqueue_to_done": round(st["max_launch_ns"] / 1e6, 3)},
+            "slowest_launch_ms": {"enqueue_to_done": round(st["max_launch_ns"] / 1e6, 3),
+                                  "enqueue": round(st["slowest_enqueue_ns"] / 1e6, 3),
+                                  "gpu_first_to_last_op": round(st["slowest_gpu_span_ns"] / 1e6, 3),
+                                  "kernel": round(st["slowest_kernel_ns"] / 1e6, 3)}}
 
 
 def throttle_delta(a, b):

@@ -75,7 +75,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint64), ("requests_done", ctypes.c_uint64), ("pixels_done", ctypes.c_uint64),
                 ("max_batch", ctypes.c_uint64), ("waiting", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64),
                 ("max_enqueue_ns", ctypes.c_uint64), ("max_kernel_ns", ctypes.c_uint64),
-                ("max_launch_ns", ctypes.c_uint64)]
+                ("max_launch_ns", ctypes.c_uint64), ("slowest_enqueue_ns", ctypes.c_uint64),
+                ("slowest_gpu_span_ns", ctypes.c_uint64), ("slowest_kernel_ns", ctypes.c_uint64)]
 
 
 class Level(ctypes.Structure):

@@ -121,6 +121,20 @@ GOOFY_FN BlockRange block_range(uint32_t mn_rb, uint32_t mn_g, uint32_t mx_rb, u
     return r;
 }
 
+// 4 * avg(avg(a, b), avg(c, d)) on both 16-bit lanes (a..d <= 255), two
+// rounding averages in one step.  With s = a + b + 1 and t = c + d + 1,
+//     avg(avg(a, b), avg(c, d)) = (s + t + 2 - (s & t & 1)) >> 2:
+// (s >> 1) + (t >> 1) = (s + t - (s & 1) - (t & 1)) / 2, and of the two
+// parities only the case of both set moves the quotient by 4.  The result
+// depends on a, b, c, d only through a + b and c + d, and the identity holds
+// for every pair of sums in 0..510.  The +2 rides in s, where it leaves s's
+// parity alone.
+GOOFY_FN uint32_t avg4_x4(uint32_t a, uint32_t b, uint32_t c, uint32_t d)
+{
+    const uint32_t s = a + b + 0x00030003u, t = c + d + 0x00010001u;
+    return (s + t - (s & t & 0x00010001u)) & 0xfffcfffcu;
+}
+
 // Channel extents of a block: R/B lane words (R in bits 0-7, B in bits
 // 16-23) and words whose byte 0 is the minimum / maximum G.
 struct Extents {
@@ -217,25 +231,20 @@ GOOFY_FN uint2 etc1s_from_extents(const uint32_t (&w)[16], const BlockLanes& l, 
     const uint32_t(&gp)[8] = l.gp;
     const BlockRange br = block_range(e.mn_rb, e.mn_g, e.mx_rb, e.mx_g);
 
-    // block mean, rounding-average tree kept exact at scale 2^level
+    // block mean, rounding-average tree kept exact at scale 2^level; the
+    // column averages and the two top levels of R / B go two levels at a
+    // time (avg4_x4, and the same identity at scale 4 below)
     uint32_t col_rb[4];
 #pragma unroll
-    for (int x = 0; x < 4; ++x) {
-        const uint32_t a = (rb[x] + rb[4 + x] + 0x00010001u) & 0xfffefffeu;
-        const uint32_t b = (rb[8 + x] + rb[12 + x] + 0x00010001u) & 0xfffefffeu;
-        col_rb[x] = (a + b + 0x00020002u) & 0xfffcfffcu;
-    }
-    const uint32_t u_rb = (col_rb[0] + col_rb[1] + 0x00040004u) & 0xfff8fff8u;
-    const uint32_t v_rb = (col_rb[2] + col_rb[3] + 0x00040004u) & 0xfff8fff8u;
-    // last level with a bias of 256 (0x1000 before the shift): lanes 256 + mean R, 256 + mean B
-    const uint32_t m_rb = ((u_rb + v_rb + 0x10081008u) & 0xfff0fff0u) >> 4;
+    for (int x = 0; x < 4; ++x) col_rb[x] = avg4_x4(rb[x], rb[4 + x], rb[8 + x], rb[12 + x]);
+    // 16 * avg(avg(c0, c1), avg(c2, c3)) for c multiples of 4, plus a bias of
+    // 256 after the shift (0x1000 in s, clear of the parity bit 2): lanes
+    // 256 + mean R, 256 + mean B
+    const uint32_t s_rb = col_rb[0] + col_rb[1] + 0x100c100cu, t_rb = col_rb[2] + col_rb[3] + 0x00040004u;
+    const uint32_t m_rb = ((s_rb + t_rb - (s_rb & t_rb & 0x00040004u)) & 0xfff0fff0u) >> 4;
     uint32_t col_g[2];
 #pragma unroll
-    for (int x = 0; x < 2; ++x) {
-        const uint32_t a = (gp[x] + gp[2 + x] + 0x00010001u) & 0xfffefffeu;
-        const uint32_t b = (gp[4 + x] + gp[6 + x] + 0x00010001u) & 0xfffefffeu;
-        col_g[x] = (a + b + 0x00020002u) & 0xfffcfffcu;  // lanes 4*col(x), 4*col(x+2)
-    }
+    for (int x = 0; x < 2; ++x) col_g[x] = avg4_x4(gp[x], gp[2 + x], gp[4 + x], gp[6 + x]);  // 4*col(x), 4*col(x+2)
     const uint32_t uv_g = (col_g[0] + col_g[1] + 0x00040004u) & 0xfff8fff8u;
     const uint32_t m_g = ((uv_g + (uv_g >> 16) + 0x1008u) & 0xfff0u) >> 4;  // 256 + mean G
 

@@ -134,8 +134,11 @@ struct LaunchSlot {
     unsigned long long* d_qsums = nullptr;  // quality: 6 error sums per request
     unsigned long long* h_qsums = nullptr;
     cudaEvent_t ev_in = nullptr, ev_kernel = nullptr;
-    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;  // timing events around the batch kernel
-    int64_t t_enqueue = 0;                         // start of this launch's enqueue (host clock)
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;        // timing events around the batch kernel
+    cudaEvent_t ev_first = nullptr, ev_last = nullptr;  // before its first and after its last GPU operation
+    int64_t t_enqueue = 0;                              // start of this launch's enqueue (host clock)
+    int64_t t_callback = 0;                             // its completion callback (host clock)
+    uint64_t enqueue_ns = 0;                            // the scheduler's time enqueueing it
     std::vector<uint64_t> tickets;
     bool busy = false;
 };
@@ -169,6 +172,7 @@ struct goofy_gpu_server {
     // stats
     uint64_t n_launches = 0, n_requests_done = 0, max_batch = 0, pixels_done = 0;
     uint64_t max_enqueue_ns = 0, max_kernel_ns = 0, max_launch_ns = 0;  // since the last stats read
+    uint64_t slowest_enqueue_ns = 0, slowest_gpu_span_ns = 0, slowest_kernel_ns = 0;  // of the max_launch_ns one
     int error = GOOFY_OK;
 
     Request& rec(uint64_t t) { return pool[t % pool.size()]; }
@@ -185,7 +189,7 @@ void CUDART_CB on_launch_done(void* p)
         std::lock_guard<std::mutex> lk(s->mu);
         LaunchSlot& sl = s->slots[a->slot];
         for (uint64_t tk : sl.tickets) s->rec(tk).t_done = t;
-        s->max_launch_ns = std::max<uint64_t>(s->max_launch_ns, (uint64_t)(t - sl.t_enqueue));
+        sl.t_callback = t;
         s->finished_slots.push_back(a->slot);
     }
     s->cv_sched.notify_one();
@@ -196,11 +200,19 @@ void retire_locked(goofy_gpu_server* s)
 {
     for (int si : s->finished_slots) {
         LaunchSlot& sl = s->slots[si];
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, sl.ev_k0, sl.ev_k1) == cudaSuccess)
-            s->max_kernel_ns = std::max<uint64_t>(s->max_kernel_ns, (uint64_t)(ms * 1e6f));
-        else
+        // timing of the finished launch (CUDA calls are not allowed in the callback, so here)
+        float k_ms = 0.f, span_ms = 0.f;
+        if (cudaEventElapsedTime(&k_ms, sl.ev_k0, sl.ev_k1) != cudaSuccess ||
+            cudaEventElapsedTime(&span_ms, sl.ev_first, sl.ev_last) != cudaSuccess)
             cudaGetLastError();
+        const uint64_t kernel_ns = (uint64_t)(k_ms * 1e6f), total_ns = (uint64_t)(sl.t_callback - sl.t_enqueue);
+        s->max_kernel_ns = std::max(s->max_kernel_ns, kernel_ns);
+        if (total_ns > s->max_launch_ns) {
+            s->max_launch_ns = total_ns;
+            s->slowest_enqueue_ns = sl.enqueue_ns;
+            s->slowest_gpu_span_ns = (uint64_t)(span_ms * 1e6f);
+            s->slowest_kernel_ns = kernel_ns;
+        }
         for (size_t i = 0; i < sl.tickets.size(); ++i) {
             Request& r = s->rec(sl.tickets[i]);
             if (s->cfg.quality) {
@@ -286,6 +298,7 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
         }
         units += ((uint64_t)bw * bh + s->tile.unit_blocks - 1) / s->tile.unit_blocks;
     }
+    GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_first, staged ? s->s_copy : s->s_compute));
     if (staged) {
         for (uint64_t tk : tickets) {
             Request& r = s->rec(tk);
@@ -325,9 +338,12 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
         }
         last = s->s_back;
     }
+    GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_last, last));
+    sl.enqueue_ns = 0;  // set below, before the scheduler can retire this launch
     GOOFY_CUDA_TRY(cudaLaunchHostFunc(last, on_launch_done, cb));
     const uint64_t enq = (uint64_t)(now_ns() - t);
     std::lock_guard<std::mutex> lk(s->mu);
+    sl.enqueue_ns = enq;
     s->max_enqueue_ns = std::max(s->max_enqueue_ns, enq);
     return GOOFY_OK;
 }
@@ -417,6 +433,8 @@ int init_server(goofy_gpu_server* s)
         GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_kernel, cudaEventDisableTiming));
         GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k0));
         GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k1));
+        GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_first));
+        GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_last));
     }
     s->resident_ctas = goofy_gpu::batch_resident_ctas(s->tile.threads, s->tile.bpt);
     s->pool.resize(c.max_requests);
@@ -440,6 +458,8 @@ void teardown(goofy_gpu_server* s)
         if (sl.ev_kernel) cudaEventDestroy(sl.ev_kernel);
         if (sl.ev_k0) cudaEventDestroy(sl.ev_k0);
         if (sl.ev_k1) cudaEventDestroy(sl.ev_k1);
+        if (sl.ev_first) cudaEventDestroy(sl.ev_first);
+        if (sl.ev_last) cudaEventDestroy(sl.ev_last);
     }
     if (s->arena_mem) cudaFree(s->arena_mem);
     for (cudaStream_t st : {s->s_copy, s->s_compute, s->s_back})
@@ -583,7 +603,11 @@ GOOFY_EXPORT int goofy_gpu_server_get_stats(goofy_gpu_server* s, goofy_gpu_serve
     st->max_enqueue_ns = s->max_enqueue_ns;
     st->max_kernel_ns = s->max_kernel_ns;
     st->max_launch_ns = s->max_launch_ns;
+    st->slowest_enqueue_ns = s->slowest_enqueue_ns;
+    st->slowest_gpu_span_ns = s->slowest_gpu_span_ns;
+    st->slowest_kernel_ns = s->slowest_kernel_ns;
     s->max_enqueue_ns = s->max_kernel_ns = s->max_launch_ns = 0;
+    s->slowest_enqueue_ns = s->slowest_gpu_span_ns = s->slowest_kernel_ns = 0;
     return GOOFY_OK;
 }
 

@@ -414,13 +414,20 @@ typedef struct goofy_gpu_request_times {
 
 typedef struct goofy_gpu_server_stats {
     uint64_t launches, requests_done, pixels_done, max_batch, waiting, inflight_bytes;
-    /* Slowest launch since the previous goofy_gpu_server_get_stats call, to
-     * tell where a late request lost its time: the scheduler thread's time
-     * in the CUDA calls that enqueue one launch (copies, kernels, callback),
-     * the GPU time of one launch's batch kernel (CUDA events around it), and
-     * the time from the start of its enqueue to its completion callback.
-     * Read and reset by each call. */
+    /* Launch timing since the previous goofy_gpu_server_get_stats call (read
+     * and reset by each call), to tell where a late request lost its time.
+     * Maxima over the launches: the scheduler thread's time in the CUDA calls
+     * that enqueue one launch (copies, kernels, callback), the GPU time of
+     * one launch's batch kernel (CUDA events around it), and the time from
+     * the start of a launch's enqueue to its completion callback. */
     uint64_t max_enqueue_ns, max_kernel_ns, max_launch_ns;
+    /* The parts of the launch that took max_launch_ns: its enqueue time, the
+     * GPU time from its first operation to its last (events on the copy /
+     * compute streams; it includes waits behind earlier launches' work once
+     * its first operation has run) and its kernel time.  What max_launch_ns
+     * has beyond the enqueue and the GPU span was spent before the GPU
+     * reached the launch or in delivering its completion callback. */
+    uint64_t slowest_enqueue_ns, slowest_gpu_span_ns, slowest_kernel_ns;
 } goofy_gpu_server_stats;
 
 /* Defaults: device 0, staged, 16 GiB budget, 1024 requests per launch, 4

@@ -155,3 +155,21 @@ def test_decoder_on_encoder_output(emu, golden, name, codec):
     want, _ = oracle.decode(codec, golden["kat_" + name], w, h)
     np.testing.assert_array_equal(got, want)
     assert bad == 0
+
+
+def test_two_level_average_identity_over_every_pair_of_sums():
+    """block_codec.cuh's avg4_x4 takes two rounding averages in one step:
+    avg(avg(a, b), avg(c, d)) = (s + t + 2 - (s & t & 1)) >> 2 with
+    s = a + b + 1, t = c + d + 1.  Both sides depend on a, b, c, d only
+    through a + b and c + d, so every pair of sums 0..510 covers every input;
+    the top level of the mean runs the same identity on multiples of 4."""
+    import numpy as np
+
+    ab = np.arange(511, dtype=np.int64)[:, None]
+    cd = np.arange(511, dtype=np.int64)[None, :]
+    want = (((ab + 1) >> 1) + ((cd + 1) >> 1) + 1) >> 1
+    s, t = ab + 1, cd + 1
+    np.testing.assert_array_equal((s + t + 2 - (s & t & 1)) >> 2, want)
+    # scaled by 4: columns c (multiples of 4 up to 1020), 16 * avg(avg(c0, c1), avg(c2, c3))
+    s4, t4 = 4 * ab + 4, 4 * cd + 4
+    np.testing.assert_array_equal((s4 + t4 + 8 - (s4 & t4 & 4)) & ~15, 16 * want)

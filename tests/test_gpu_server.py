@@ -77,8 +77,11 @@ def test_results_equal_alone_and_in_the_mix(cuda, mode, pinned):
         assert st["max_batch"] > 1 and st["inflight_bytes"] == 0
         # the slowest launch's parts: enqueue and kernel within enqueue-to-completion, all read and reset
         assert 0 < st["max_kernel_ns"] and 0 < st["max_enqueue_ns"] < st["max_launch_ns"]
+        assert 0 < st["slowest_kernel_ns"] <= st["slowest_gpu_span_ns"] and 0 < st["slowest_enqueue_ns"]
+        assert st["slowest_enqueue_ns"] <= st["max_enqueue_ns"] and st["slowest_kernel_ns"] <= st["max_kernel_ns"]
         st = srv.stats()
         assert st["max_kernel_ns"] == st["max_enqueue_ns"] == st["max_launch_ns"] == 0
+        assert st["slowest_kernel_ns"] == st["slowest_gpu_span_ns"] == st["slowest_enqueue_ns"] == 0
         # the same request served on its own gives the same bytes
         r = reqs[5]
         r["dst"][:] = 0
