@@ -837,15 +837,19 @@ def run_serving(args, g, device):
                                     "(~211 GB/s) caps serving far below the device-resident batched rate",
               "host_cpus": os.cpu_count(), "cgroup_cpu_quota": cpu_quota()}
     try:
-        for name, mode in (("staged", g.SERVER_STAGED), ("direct", g.SERVER_DIRECT)):
-            srv = g.Server(mode=mode, device=device)
+        # the direct server learns of each launch's end from a thread waiting on its last event (no host
+        # function between its launches on the one stream); the staged one from a host callback
+        for name, mode, comp in (("staged", g.SERVER_STAGED, g.COMPLETION_CALLBACK),
+                                 ("direct", g.SERVER_DIRECT, g.COMPLETION_EVENT)):
+            srv = g.Server(mode=mode, device=device, completion=comp)
             try:
                 n_sat = 20000
                 reqs, arrival, px, probe = stream(n_sat, None)
                 rc, lat, wall = srv.replay(reqs, arrival)
                 assert rc == g.OK, g.last_error()
                 cap = float(px.sum()) / (wall / 1e9)
-                entry = {"capacity_mpix_s": round(cap / 1e6, 1), "capacity_requests": n_sat,
+                entry = {"completion": "event" if comp == g.COMPLETION_EVENT else "callback",
+                         "capacity_mpix_s": round(cap / 1e6, 1), "capacity_requests": n_sat,
                          "mean_request_px": round(float(px.mean()))}
                 warm_rate = 0.1 * cap / float(px.mean())  # settle the server before the measured runs
                 reqs, arrival, _, _ = stream(max(200, int(warm_rate * 0.2)), warm_rate)

@@ -52,12 +52,14 @@ HOST_PATH_DIRECT = 2
 
 SERVER_STAGED = 0
 SERVER_DIRECT = 1
+COMPLETION_CALLBACK = 0
+COMPLETION_EVENT = 1
 
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("mode", ctypes.c_int32), ("device_budget_bytes", ctypes.c_uint64),
                 ("max_batch_images", ctypes.c_uint32), ("max_inflight_batches", ctypes.c_uint32),
-                ("max_requests", ctypes.c_uint32), ("quality", ctypes.c_uint32)]
+                ("max_requests", ctypes.c_uint32), ("quality", ctypes.c_uint32), ("completion", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -490,11 +492,14 @@ class Server:
     """goofy_gpu_server: continuous-batching server for host-memory requests."""
 
     def __init__(self, mode=SERVER_STAGED, device_budget_bytes=16 << 30, max_batch_images=1024,
-                 max_inflight_batches=4, max_requests=1 << 20, device=0, quality=False):
+                 max_inflight_batches=4, max_requests=1 << 20, device=0, quality=False,
+                 completion=None):
         cfg = ServerConfig()
         lib().goofy_gpu_server_default_config(ctypes.byref(cfg))
         cfg.device, cfg.mode, cfg.device_budget_bytes = device, mode, device_budget_bytes
         cfg.quality = 1 if quality else 0
+        if completion is not None:
+            cfg.completion = completion
         cfg.max_batch_images, cfg.max_inflight_batches, cfg.max_requests = (max_batch_images, max_inflight_batches,
                                                                             max_requests)
         h = ctypes.c_void_p()

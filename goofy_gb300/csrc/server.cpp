@@ -21,7 +21,9 @@
 //     sums the harness's squared errors per request (same work units, one
 //     more launch), so every request also gets its RGB PSNR,
 //   * releases arena space and launch slots when a launch's completion
-//     callback fires (cudaLaunchHostFunc), which also timestamps the requests.
+//     callback fires (cudaLaunchHostFunc), which also timestamps the requests
+//     -- or, with config.completion = EVENT, when a thread of the server that
+//     waits on each launch's last event in turn sees it complete.
 // A batch of size 1 with one launch slot is the plain one-request-per-launch
 // loop, used as the baseline.
 #include <cuda_runtime.h>
@@ -149,9 +151,11 @@ struct goofy_gpu_server {
     goofy_gpu_server_config cfg{};
     BatchTile tile{128, 1, 256};
     std::mutex mu;
-    std::condition_variable cv_sched, cv_done;
-    std::thread sched;
+    std::condition_variable cv_sched, cv_done, cv_poll;
+    std::thread sched, poller;
     bool stop = false;
+    bool stop_poller = false;
+    std::deque<int> polling;  // COMPLETION_EVENT: launch slots in flight, in launch order
 
     std::vector<Request> pool;  // ring of request records, indexed by ticket % size
     uint64_t next_ticket = 1;
@@ -180,6 +184,16 @@ struct goofy_gpu_server {
 
 namespace {
 
+// A launch finished at host time t: stamp its requests and hand the slot to
+// the scheduler (lock held).
+void finish_launch_locked(goofy_gpu_server* s, int slot, int64_t t)
+{
+    LaunchSlot& sl = s->slots[slot];
+    for (uint64_t tk : sl.tickets) s->rec(tk).t_done = t;
+    sl.t_callback = t;
+    s->finished_slots.push_back(slot);
+}
+
 void CUDART_CB on_launch_done(void* p)
 {
     CallbackArg* a = static_cast<CallbackArg*>(p);
@@ -187,10 +201,7 @@ void CUDART_CB on_launch_done(void* p)
     const int64_t t = now_ns();
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        LaunchSlot& sl = s->slots[a->slot];
-        for (uint64_t tk : sl.tickets) s->rec(tk).t_done = t;
-        sl.t_callback = t;
-        s->finished_slots.push_back(a->slot);
+        finish_launch_locked(s, a->slot, t);
     }
     s->cv_sched.notify_one();
 }
@@ -339,13 +350,43 @@ int launch(goofy_gpu_server* s, int si, const std::vector<uint64_t>& tickets, Ca
         last = s->s_back;
     }
     GOOFY_CUDA_TRY(cudaEventRecord(sl.ev_last, last));
-    sl.enqueue_ns = 0;  // set below, before the scheduler can retire this launch
-    GOOFY_CUDA_TRY(cudaLaunchHostFunc(last, on_launch_done, cb));
+    const bool poll = s->cfg.completion == GOOFY_SERVER_COMPLETION_EVENT;  // a server thread waits on ev_last
+    if (!poll) GOOFY_CUDA_TRY(cudaLaunchHostFunc(last, on_launch_done, cb));
     const uint64_t enq = (uint64_t)(now_ns() - t);
-    std::lock_guard<std::mutex> lk(s->mu);
-    sl.enqueue_ns = enq;
-    s->max_enqueue_ns = std::max(s->max_enqueue_ns, enq);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        sl.enqueue_ns = enq;  // the scheduler retires this launch only after launch() returns
+        s->max_enqueue_ns = std::max(s->max_enqueue_ns, enq);
+        if (poll) s->polling.push_back(cb->slot);
+    }
+    if (poll) s->cv_poll.notify_one();
     return GOOFY_OK;
+}
+
+// COMPLETION_EVENT: waits for the launches in flight in launch order (they
+// finish in that order: each stream runs its part of the launches in turn)
+// on each one's last event, a blocking-sync event: the thread sleeps until
+// the GPU has passed it.
+void poller_main(goofy_gpu_server* s)
+{
+    cudaSetDevice(s->cfg.device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        if (s->polling.empty()) {
+            if (s->stop_poller) break;
+            s->cv_poll.wait_for(lk, std::chrono::milliseconds(2));
+            continue;
+        }
+        const int si = s->polling.front();
+        const cudaEvent_t ev = s->slots[si].ev_last;
+        lk.unlock();
+        if (cudaEventSynchronize(ev) != cudaSuccess) cudaGetLastError();  // a failed launch still releases its slot
+        const int64_t t = now_ns();
+        lk.lock();
+        s->polling.pop_front();
+        finish_launch_locked(s, si, t);
+        s->cv_sched.notify_one();
+    }
 }
 
 void scheduler_main(goofy_gpu_server* s)
@@ -434,7 +475,7 @@ int init_server(goofy_gpu_server* s)
         GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k0));
         GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_k1));
         GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_first));
-        GOOFY_CUDA_TRY(cudaEventCreate(&sl.ev_last));
+        GOOFY_CUDA_TRY(cudaEventCreateWithFlags(&sl.ev_last, cudaEventBlockingSync));
     }
     s->resident_ctas = goofy_gpu::batch_resident_ctas(s->tile.threads, s->tile.bpt);
     s->pool.resize(c.max_requests);
@@ -487,7 +528,7 @@ GOOFY_EXPORT int goofy_gpu_server_create(goofy_gpu_server** out, const goofy_gpu
     if (!out || !cfg) return GOOFY_ERR_INVALID;
     *out = nullptr;
     if (cfg->mode != GOOFY_SERVER_STAGED && cfg->mode != GOOFY_SERVER_DIRECT) return GOOFY_ERR_INVALID;
-    if (cfg->quality > 1) return GOOFY_ERR_INVALID;
+    if (cfg->quality > 1 || cfg->completion > GOOFY_SERVER_COMPLETION_EVENT) return GOOFY_ERR_INVALID;
     if (cfg->device_budget_bytes < (1u << 20) || cfg->max_batch_images == 0 || cfg->max_batch_images > 65536 ||
         cfg->max_inflight_batches == 0 || cfg->max_inflight_batches > 64 || cfg->max_requests < 16)
         return GOOFY_ERR_INVALID;
@@ -504,6 +545,7 @@ GOOFY_EXPORT int goofy_gpu_server_create(goofy_gpu_server** out, const goofy_gpu
         delete s;
         return rc;
     }
+    if (s->cfg.completion == GOOFY_SERVER_COMPLETION_EVENT) s->poller = std::thread(poller_main, s);
     s->sched = std::thread(scheduler_main, s);
     *out = s;
     return GOOFY_OK;
@@ -517,7 +559,13 @@ GOOFY_EXPORT void goofy_gpu_server_destroy(goofy_gpu_server* s)
         s->stop = true;
     }
     s->cv_sched.notify_all();
-    if (s->sched.joinable()) s->sched.join();
+    if (s->sched.joinable()) s->sched.join();  // returns once every launch has completed
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop_poller = true;
+    }
+    s->cv_poll.notify_all();
+    if (s->poller.joinable()) s->poller.join();
     teardown(s);
     delete s;
 }

@@ -386,6 +386,14 @@ int goofy_gpu_batch_autotune(goofy_gpu_batch* batch, const goofy_gpu_image* imag
 #define GOOFY_SERVER_STAGED 0 /* requests copied into a device arena, encoded there, copied back */
 #define GOOFY_SERVER_DIRECT 1 /* the batch kernel reads / writes the requests' host buffers itself */
 
+/* How the server learns that a launch has finished. */
+#define GOOFY_SERVER_COMPLETION_CALLBACK 0 /* a host function enqueued after the launch (cudaLaunchHostFunc),
+                                            * run by the CUDA driver's thread; it also holds back the next
+                                            * launch's work on that stream until it has run */
+#define GOOFY_SERVER_COMPLETION_EVENT 1    /* a thread of the server waits on each launch's last event in
+                                            * turn (a blocking-sync event: the thread sleeps, no spinning);
+                                            * nothing is added to the streams */
+
 typedef struct goofy_gpu_server goofy_gpu_server;
 
 typedef struct goofy_gpu_server_config {
@@ -396,6 +404,7 @@ typedef struct goofy_gpu_server_config {
     uint32_t max_inflight_batches; /* launches on the GPU at once */
     uint32_t max_requests;         /* unreleased tickets at once */
     uint32_t quality;              /* 1: measure every request's RGB PSNR on the GPU (harness's getMsePsnr) */
+    uint32_t completion;           /* GOOFY_SERVER_COMPLETION_CALLBACK (default) or _EVENT */
 } goofy_gpu_server_config;
 
 /* One encode request on host memory (pinned buffers are copied by DMA / read

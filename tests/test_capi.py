@@ -107,3 +107,17 @@ def test_tile_get_set(built):
     assert g.set_tile(g.CODEC_BOTH, 256, 4, 0) == g.ERR_INVALID
     assert g.set_tile(g.CODEC_BOTH, *before) == g.OK
     assert g.set_tile(3, 256, 2, 0) == g.ERR_INVALID
+
+
+def test_server_config_checks_before_cuda(built):
+    """goofy_gpu_server_create rejects a bad config before touching CUDA."""
+    cfg = g.ServerConfig()
+    g.lib().goofy_gpu_server_default_config(ctypes.byref(cfg))
+    assert cfg.completion == g.COMPLETION_CALLBACK and cfg.mode == g.SERVER_STAGED
+    h = ctypes.c_void_p()
+    for field, bad in (("completion", 2), ("mode", 5), ("quality", 2), ("max_batch_images", 0)):
+        c = g.ServerConfig()
+        g.lib().goofy_gpu_server_default_config(ctypes.byref(c))
+        setattr(c, field, bad)
+        assert g.lib().goofy_gpu_server_create(ctypes.byref(h), ctypes.byref(c)) == g.ERR_INVALID, field
+        assert not h.value

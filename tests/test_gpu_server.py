@@ -137,13 +137,17 @@ def test_ticket_ring_and_argument_checks(cuda):
         free_requests(reqs)
 
 
+@pytest.mark.parametrize("completion", [g.COMPLETION_CALLBACK, g.COMPLETION_EVENT])
 @pytest.mark.parametrize("mode", [g.SERVER_STAGED, g.SERVER_DIRECT])
-def test_replay_and_plain_loop(cuda, mode):
+def test_replay_and_plain_loop(cuda, mode, completion):
+    """Open-loop replay through the server (a launch's completion seen by a
+    host callback, or by the server's thread waiting on its last event) and through the plain
+    loop: every request's blocks equal its encode alone."""
     rng = np.random.default_rng(21)
     reqs = make_requests(rng, 64, True, max_side=512)
     arr = g.requests_array([(r["src"], r["dst"], r["w"], r["h"], r["stride"], r["codec"]) for r in reqs])
     arrival = np.cumsum(rng.exponential(20e3, len(reqs))).astype(np.int64)  # ~50k requests/s
-    srv = g.Server(mode=mode)
+    srv = g.Server(mode=mode, completion=completion)
     try:
         rc, lat, wall, stamps = srv.replay(arr, arrival, with_times=True)
         assert rc == g.OK and (lat > 0).all() and wall > 0
