@@ -224,3 +224,44 @@ def test_full_mixed_batch_1000_textures(cuda):
         want = oracle.encode(lv["codec"], lv["pixels"], lv["width"], lv["height"], threads=0 if n > 65536 else 1)
         for out in outs:
             np.testing.assert_array_equal(out[o:o + n], want)
+
+
+@pytest.mark.parametrize("tile", [(512, 2, 1024, 1), (256, 1, 256, 1)])
+def test_pipelined_batches_keep_stream_order(cuda, tile):
+    """Pipelined batch launches (programmatic dependent launch, and an L2
+    prefetch of their first rows before the dependency wait) back to back on
+    one stream with an image kernel, each touching memory the previous launch
+    reads or writes, without synchronisation:
+      X (image kernel) writes blocks into P;
+      A (batch) encodes P's bytes as an image (reads what X wrote) into Q,
+        and `img` into R;
+      B (batch) overwrites `img`, which A read;
+      C (batch) encodes again into R, which A wrote."""
+    w, h = 1024, 512
+    img = workloads.scene(w, h, 8)
+    other = workloads.stress(w, h, 9)
+    n = g.out_size(w, h)
+    st = cuda.cuda.current_stream().cuda_stream
+    src = cuda.from_numpy(img.reshape(-1)).cuda()
+    oth = cuda.from_numpy(other.reshape(-1)).cuda()
+    p = cuda.zeros(n, dtype=cuda.uint8, device="cuda")  # X's blocks (256 KiB), read by A as a 256x256 RGBA image
+    q = cuda.zeros(g.out_size(256, 256), dtype=cuda.uint8, device="cuda")
+    r = cuda.zeros(n, dtype=cuda.uint8, device="cuda")
+    b = g.Batch(4)
+    try:
+        assert b.set_tile(*tile) == g.OK
+        cuda.cuda.synchronize()
+        assert g.compress_device(g.CODEC_ETC1S, p.data_ptr(), src.data_ptr(), w, h, 4 * w, st) == g.OK      # X
+        assert b.encode([(p, q, 256, 256, 1024, g.CODEC_BC1), (src, r, w, h, 4 * w, g.CODEC_BC1)], st) == g.OK  # A
+        assert b.encode([(oth, src, w, h, 4 * w, g.CODEC_ETC1S)], st) == g.OK                              # B
+        assert b.encode([(oth, r, w, h, 4 * w, g.CODEC_ETC1S)], st) == g.OK                                # C
+        cuda.cuda.synchronize()
+    finally:
+        b.close()
+    x_blocks = oracle.encode(g.CODEC_ETC1S, img, w, h)
+    np.testing.assert_array_equal(p.cpu().numpy(), x_blocks)
+    np.testing.assert_array_equal(q.cpu().numpy(),
+                                  oracle.encode(g.CODEC_BC1, x_blocks.reshape(256, 1024), 256, 256))
+    want_b = oracle.encode(g.CODEC_ETC1S, other, w, h)
+    np.testing.assert_array_equal(src[:n].cpu().numpy(), want_b)
+    np.testing.assert_array_equal(r.cpu().numpy(), want_b)
