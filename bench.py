@@ -1140,6 +1140,9 @@ def run_gpu(args):
             g.host_free(p_out)
 
     if rank != 0:
+        import shutil
+
+        shutil.rmtree(cache_dir, ignore_errors=True)
         torch.distributed.destroy_process_group()
         return 0
 
@@ -1216,6 +1219,10 @@ def run_gpu(args):
             "clocks": dict(clocks.summary(), window="timed region + %.1f s soak of the same loop" % args.soak_s),
             "gpu_launches": 2 * args.steps}
     line["summary"] = summary(line, peak)
+    import shutil
+
+    g.set_tile_cache_path(None)
+    shutil.rmtree(cache_dir, ignore_errors=True)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
