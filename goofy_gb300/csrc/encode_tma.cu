@@ -70,6 +70,48 @@ __host__ __device__ constexpr TmaLayout tma_layout(uint32_t compute_threads, uin
 
 constexpr size_t tma_smem_bytes(const TmaLayout& l) { return (size_t)l.stages * (l.stage_bytes + 16u) + 128u; }
 
+// Encodes the blocks of one stage held in shared memory (4 rows of
+// row_bytes, block b at 16 * b in each) and stores those below nb at
+// out + 8 * b (and out2, for both codecs).  Thread `lane` of compute warp
+// `warp` takes blocks (warp * BPT + j) * 32 + lane.  Every thread loads and
+// encodes all its slots, also past nb (a narrower tile at the right edge):
+// such a slot holds whatever an earlier tile left in the stage, which
+// nothing writes while the stage is held, and its result is dropped.  Only
+// the stores are conditional, so the loads and the codec run without
+// branches.
+template <int CODEC, int BPT>
+__device__ __forceinline__ void encode_stage(const uint8_t* buf, uint32_t row_bytes, uint32_t warp, uint32_t lane,
+                                             uint32_t nb, uint8_t* out, uint8_t* out2, const uint8_t* ctrl_lut)
+{
+    uint32_t w[BPT][16];
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t b = (warp * BPT + j) * 32u + lane;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint4 v = *reinterpret_cast<const uint4*>(buf + r * row_bytes + 16u * b);
+            w[j][4 * r + 0] = v.x;
+            w[j][4 * r + 1] = v.y;
+            w[j][4 * r + 2] = v.z;
+            w[j][4 * r + 3] = v.w;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) {
+        const uint32_t b = (warp * BPT + j) * 32u + lane;
+        if constexpr (CODEC == kBoth) {
+            const uint4 e = encode_both(w[j], ctrl_lut);
+            if (b < nb) {
+                st_stream8(out + 8u * (size_t)b, make_uint2(e.x, e.y));
+                st_stream8(out2 + 8u * (size_t)b, make_uint2(e.z, e.w));
+            }
+        } else {
+            const uint2 e = encode_block<CODEC>(w[j], ctrl_lut);
+            if (b < nb) st_stream8(out + 8u * (size_t)b, e);
+        }
+    }
+}
+
 template <int CODEC, int BPT, int COMPUTE>
 __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     encode_image_tma(const uint8_t* __restrict__ src, size_t stride, uint8_t* __restrict__ dst,
@@ -156,35 +198,10 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
         const uint32_t bx0 = tx * L.tile_blocks;
         const uint32_t nb = min(L.tile_blocks, bw - bx0);
         const uint8_t* buf = smem + slot * L.stage_bytes;
-        uint32_t w[BPT][16];
-#pragma unroll
-        for (int j = 0; j < BPT; ++j) {
-            const uint32_t b = (warp * BPT + j) * 32u + lane;
-            if (b < nb) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const uint4 v = *reinterpret_cast<const uint4*>(buf + r * L.row_bytes + 16u * b);
-                    w[j][4 * r + 0] = v.x;
-                    w[j][4 * r + 1] = v.y;
-                    w[j][4 * r + 2] = v.z;
-                    w[j][4 * r + 3] = v.w;
-                }
-            }
-        }
         const size_t o = ((size_t)by * bw + bx0) * 8u;
-#pragma unroll
-        for (int j = 0; j < BPT; ++j) {
-            const uint32_t b = (warp * BPT + j) * 32u + lane;
-            if (b < nb) {
-                if constexpr (CODEC == kBoth) {
-                    const uint4 e = encode_both(w[j], ctrl_lut);
-                    st_stream8(dst + o + 8u * (size_t)b, make_uint2(e.x, e.y));
-                    st_stream8(dst2 + o + 8u * (size_t)b, make_uint2(e.z, e.w));
-                } else {
-                    st_stream8(dst + o + 8u * (size_t)b, encode_block<CODEC>(w[j], ctrl_lut));
-                }
-            }
-        }
+        if (warp * (BPT * 32u) < nb)  // warps wholly past a narrower tile's last block skip it
+            encode_stage<CODEC, BPT>(buf, L.row_bytes, warp, lane, nb, dst + o,
+                                     CODEC == kBoth ? dst2 + o : nullptr, ctrl_lut);
         // Release the stage only now.  An arrival right after the shared loads
         // can overtake them: the loads wait in the load/store queue (behind
         // other kernels' global loads when SMs are shared) while the arrival
