@@ -755,7 +755,7 @@ def run_serving(args, g, device):
     the mixed batch's texture levels plus a 1024x1024 probe class at 10% of
     arrivals, BC1 / ETC1s 50/50, pinned inputs and outputs), offered at
     10/25/50/75/90% of the server's measured capacity.  Capacity = the same
-    request mix all arriving at once.  Both data paths of the server are run;
+    request mix all arriving at once (best of three runs, after a warm-up).  Both data paths of the server are run;
     the plain loop (one request per launch, sequential) is the baseline."""
     import numpy as np
 
@@ -845,11 +845,16 @@ def run_serving(args, g, device):
             try:
                 n_sat = 20000
                 reqs, arrival, px, probe = stream(n_sat, None)
-                rc, lat, wall = srv.replay(reqs, arrival)
-                assert rc == g.OK, g.last_error()
-                cap = float(px.sum()) / (wall / 1e9)
+                assert srv.replay(reqs[:2000], arrival[:2000])[0] == g.OK  # the server's first launches
+                caps = []
+                for _ in range(3):
+                    rc, lat, wall = srv.replay(reqs, arrival)
+                    assert rc == g.OK, g.last_error()
+                    caps.append(float(px.sum()) / (wall / 1e9))
+                cap = max(caps)
                 entry = {"completion": "event" if comp == g.COMPLETION_EVENT else "callback",
                          "capacity_mpix_s": round(cap / 1e6, 1), "capacity_requests": n_sat,
+                         "capacity_runs_mpix_s": [round(c / 1e6, 1) for c in caps],
                          "mean_request_px": round(float(px.mean()))}
                 warm_rate = 0.1 * cap / float(px.mean())  # settle the server before the measured runs
                 reqs, arrival, _, _ = stream(max(200, int(warm_rate * 0.2)), warm_rate)
@@ -910,6 +915,7 @@ def run_serving(args, g, device):
             srv.close()
         n_plain = 4000
         reqs, arrival, px, probe = stream(n_plain, None)
+        assert g.plain_replay(reqs[:400], arrival[:400], device)[0] == g.OK
         rc, lat, wall = g.plain_replay(reqs, arrival, device)
         assert rc == g.OK, g.last_error()
         plain_cap = float(px.sum()) / (wall / 1e9)
