@@ -162,6 +162,58 @@ def test_full_size_stress_4096(cuda, name, codec):
         np.testing.assert_array_equal(part.reshape(h // 4, q // 4, 8), full[:, k * q // 4:(k + 1) * q // 4])
 
 
+def test_image_larger_than_4_gib(cuda):
+    """A 32772x32768 image (4,295,491,584 bytes, past 2^32, rows of 131,088
+    bytes, 8193 blocks a row so every row of tiles ends in a one-block tile):
+    the single-codec kernels (bulk-copy ring and register-loading grid), the
+    two-codec pass and a one-image batch all match the oracle.  Each row's
+    content differs (a band of noise XOR a per-row byte), so a block read
+    from a wrapped 32-bit offset would not match."""
+    w, h = 32772, 32768
+    stride = 4 * w
+    assert stride * h > 1 << 32
+    rng = np.random.default_rng(42)
+    band = rng.integers(0, 256, (64, stride), dtype=np.uint8)
+    img = np.tile(band, (h // 64, 1))
+    img ^= ((np.arange(h, dtype=np.uint64) * 2654435761) >> np.uint64(7)).astype(np.uint8)[:, None]
+    want = [oracle.encode(c, img, w, h, threads=0) for c in (g.CODEC_BC1, g.CODEC_ETC1S)]
+    src = cuda.from_numpy(img.reshape(-1)).cuda()
+    del img
+    n = g.out_size(w, h)
+    out = cuda.empty(2 * n, dtype=cuda.uint8, device="cuda")
+    stream = cuda.cuda.current_stream().cuda_stream
+
+    def check(k, label):
+        cuda.cuda.synchronize()
+        got = out[k * n:(k + 1) * n].cpu().numpy()
+        assert np.array_equal(got, want[k]), label
+
+    for c in (g.CODEC_BC1, g.CODEC_ETC1S):
+        before = g.get_tile(c)
+        try:
+            for tile in (before, (128, 2, 0)):
+                assert g.set_tile(c, *tile) == g.OK
+                out.fill_(0)
+                assert g.compress_device(c, out[c * n:].data_ptr(), src.data_ptr(), w, h, stride, stream) == g.OK
+                check(c, (c, tile))
+        finally:
+            g.set_tile(c, *before)
+    out.fill_(0)
+    assert g.compress_both_device(out.data_ptr(), out[n:].data_ptr(), src.data_ptr(), w, h, stride, stream) == g.OK
+    check(0, "both, bc1")
+    check(1, "both, etc1s")
+    b = g.Batch(2)
+    try:
+        out.fill_(0)
+        assert b.encode([(src, out[:n], w, h, stride, g.CODEC_BC1), (src, out[n:], w, h, stride, g.CODEC_ETC1S)],
+                        stream) == g.OK
+        check(0, "batch, bc1")
+        check(1, "batch, etc1s")
+    finally:
+        b.close()
+    assert g.pipeline_timeouts() == 0
+
+
 def test_concurrent_kernels_bit_exact(cuda):
     """The two codecs on two streams at once, one through the bulk-copy
     pipeline and the other through a register-loading kernel sharing its SMs
