@@ -303,7 +303,6 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
     int rc = GOOFY_OK;
     BatchTile best_tile{0, 0, 0, 0};
     float best_time = 0.f;
-    std::vector<float> t(reps);
     std::vector<BatchTile> candidates;
     for (uint32_t threads : {128u, 256u, 512u})
         for (uint32_t bpt : {1u, 2u}) {
@@ -311,15 +310,21 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
                 candidates.push_back(BatchTile{threads, bpt, unit, 0});
             candidates.push_back(BatchTile{threads, bpt, threads * bpt, 1});  // the pipelined kernel: a unit per stage
         }
+    // Per tile: two warm-up launches, then three rounds of `reps` launches
+    // back to back between two events (no event between launches, so each
+    // can overlap the previous one's tail as a caller's stream of batches
+    // does); the median round's mean per launch.
     for (const BatchTile& tile : candidates) {
         if (!goofy_gpu::batch_tile_valid(tile)) continue;
-        for (uint32_t r = 0; r < reps + 1 && rc == GOOFY_OK; ++r) {
+        for (uint32_t w = 0; w < 2 && rc == GOOFY_OK; ++w) rc = encode_locked(b, images, count, b->stream, tile);
+        float t[3] = {0.f, 0.f, 0.f};
+        for (int r = 0; r < 3 && rc == GOOFY_OK; ++r) {
             cudaError_t e = cudaEventRecord(ev[0], b->stream);
             if (e != cudaSuccess) {
                 rc = cuda_fail(e, "cudaEventRecord");
                 break;
             }
-            rc = encode_locked(b, images, count, b->stream, tile);
+            for (uint32_t k = 0; k < reps && rc == GOOFY_OK; ++k) rc = encode_locked(b, images, count, b->stream, tile);
             if (rc != GOOFY_OK) break;
             e = cudaEventRecord(ev[1], b->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
@@ -329,11 +334,11 @@ GOOFY_EXPORT int goofy_gpu_batch_autotune(goofy_gpu_batch* b, const goofy_gpu_im
                 rc = cuda_fail(e, "autotune timing");
                 break;
             }
-            if (r > 0) t[r - 1] = ms;  // the first launch is a warm-up
+            t[r] = ms / (float)reps;
         }
         if (rc != GOOFY_OK) break;
-        std::sort(t.begin(), t.end());
-        const float med = t[reps / 2];
+        std::sort(t, t + 3);
+        const float med = t[1];
         if (best_tile.threads == 0 || med < best_time) {
             best_time = med;
             best_tile = tile;

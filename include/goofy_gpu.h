@@ -375,9 +375,10 @@ int goofy_gpu_batch_set_graphs(goofy_gpu_batch* batch, int enable);
 int goofy_gpu_batch_get_tile(goofy_gpu_batch* batch, goofy_gpu_batch_tile* tile);
 int goofy_gpu_batch_set_tile(goofy_gpu_batch* batch, const goofy_gpu_batch_tile* tile);
 
-/* Time every batch tile on this set of images (CUDA events, `reps` timed
- * launches each, median), keep the fastest for this batch object.  Writes
- * the images' outputs as a side effect.  Synchronous. */
+/* Time every batch tile on this set of images, keep the fastest for this
+ * batch object: per tile two warm-up launches, then three rounds of `reps`
+ * launches back to back between two CUDA events, the median round's mean
+ * per launch.  Writes the images' outputs as a side effect.  Synchronous. */
 int goofy_gpu_batch_autotune(goofy_gpu_batch* batch, const goofy_gpu_image* images, uint32_t count, uint32_t reps,
                              goofy_gpu_batch_tile* best, float* best_us);
 
