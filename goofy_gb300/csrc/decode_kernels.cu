@@ -13,6 +13,8 @@
 // shuffles and shared memory, one 64-bit atomic per CTA and channel).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "batch.h"
 #include "block_codec.cuh"
 #include "block_decode.cuh"
@@ -102,12 +104,14 @@ __device__ __forceinline__ uint32_t luma_row(const uint32_t (&a)[4], const uint3
 
 // Resident grid: each thread walks blocks with a grid stride, keeps 64-bit
 // sums, then the CTA reduces (shuffles, shared memory) and adds its six
-// totals with one atomic each.
+// totals with one atomic each.  Register caps for 4 (BC1, 64 registers) /
+// 3 (ETC1, 80) CTAs per SM, no spills: uncapped, ETC1 took 94 registers and
+// 2 CTAs per SM (51.3 against 47.4 us at 8192^2); capped at 4 CTAs it
+// spilled (50.9 us).
 template <int CODEC>
-__global__ void __launch_bounds__(kDecodeThreads) block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw,
-                                                          uint32_t nblk, const uint8_t* __restrict__ src,
-                                                          size_t stride, bool vec16,
-                                                          unsigned long long* __restrict__ sums)
+__global__ void __launch_bounds__(kDecodeThreads, CODEC == kBC1 ? 4 : 3)
+    block_error_kernel(const uint8_t* __restrict__ blocks, uint32_t bw, uint32_t nblk, const uint8_t* __restrict__ src,
+                       size_t stride, bool vec16, unsigned long long* __restrict__ sums)
 {
     pdl_launch_dependents();
     __shared__ uint32_t pal[8 * kDecodeThreads];
@@ -248,6 +252,30 @@ cudaError_t launch_decode(int codec, const uint8_t* blocks, uint32_t width, uint
                       unsupported);
 }
 
+namespace {
+
+// Resident CTAs of `kernel` per SM on device `dev` (cached per device and
+// slot), at least 1.
+template <typename K>
+uint32_t resident_per_sm(K kernel, int dev, int slot)
+{
+    static std::atomic<uint32_t> cache[64][2];
+    if (dev < 0 || dev >= 64) dev = 0;
+    uint32_t n = cache[dev][slot].load(std::memory_order_relaxed);
+    if (n == 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kDecodeThreads, 0) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 0;
+        }
+        n = per_sm > 0 ? (uint32_t)per_sm : 1u;
+        cache[dev][slot].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+}  // namespace
+
 cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* src, uint32_t width, uint32_t height,
                                size_t stride, bool vec16, unsigned long long* sums, cudaStream_t stream)
 {
@@ -256,7 +284,13 @@ cudaError_t launch_block_error(int codec, const uint8_t* blocks, const uint8_t* 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t grid = min((nblk + kDecodeThreads - 1) / kDecodeThreads, (uint32_t)(sms > 0 ? sms : 1) * 8u);
+    // One wave: as many CTAs as fit on the GPU at once, each thread striding
+    // over its share of the blocks.  A grid of 8 CTAs per SM ran in 2.7
+    // waves for BC1 and left SMs part-empty in the last one (50.6 against
+    // 47.2 us at 8192^2).
+    const uint32_t per_sm = codec == kBC1 ? resident_per_sm(block_error_kernel<kBC1>, dev, 0)
+                                          : resident_per_sm(block_error_kernel<kETC1S>, dev, 1);
+    const uint32_t grid = min((nblk + kDecodeThreads - 1) / kDecodeThreads, (uint32_t)(sms > 0 ? sms : 1) * per_sm);
     if (codec == kBC1)
         return launch_pdl(block_error_kernel<kBC1>, dim3(grid), dim3(kDecodeThreads), 0, stream, blocks, bw, nblk, src, stride,
                           vec16, sums);
