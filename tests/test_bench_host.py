@@ -175,7 +175,7 @@ def test_small_configs_bookkeeping():
     small = [c for c in calls if c[3] == 256]
     assert len(big) == 2 * (2 + 3 * n) + (2 + 3 * n) and {s for *_, s in big} == {16384}
     assert len({c[2] for c in big}) == 4 and len({c[1] for c in big}) == 4  # 4 inputs, 4 outputs
-    assert len(small) == 2 * (22 + 2 + 3 * 200) and {s for *_, s in small} == {1024}
+    assert len(small) == 2 * (62 + 2 + 3 * 200) and {s for *_, s in small} == {1024}
     r = res["4096x4096"]["etc1s"]
     assert r["mean_launch_us"] == round(5.0 / n, 2)  # one 5 us tick of the fake clock over n launches
     assert r["frac"] == round(4.5 * 4096 * 4096 / (5.0 / n) / 1e3 / 6800.0, 4)
