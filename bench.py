@@ -471,9 +471,9 @@ def run_small_configs(args, g, torch, workloads, codecs, stream, peak):
         small[names[c]] = {"latency_us": round(statistics.mean(ts), 2), "latency_median_us": round(statistics.median(ts), 2),
                            "latency_min_us": round(min(ts), 2), "back_to_back_us": round(b2b, 2)}
     small["timing"] = ("latency: one launch between its own two CUDA events after a 256 MiB write (L2 cold), mean of "
-                       "60 (the event timestamps step by about 2 us, so single values and their median sit on that "
-                       "grid; the mean of many does not); back_to_back: mean of 200 launches between two events (input "
-                       "L2-resident)")
+                       "60; such an event pair reads in steps of about 2 us on this GPU, the same step in every repeat, "
+                       "so this is an upper bound at that resolution; back_to_back: mean of 200 launches between two "
+                       "events (input L2-resident)")
     del flush
     return {"4096x4096": stress, "256x256": small}
 
