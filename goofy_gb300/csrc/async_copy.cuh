@@ -56,6 +56,27 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         : "memory");
 }
 
+// An L2 cache policy for data read once: its lines are the first L2 gives
+// up when it needs room, so they do not push out lines still wanted (the
+// rows the next launch prefetched, blocks not yet written back).
+__device__ __forceinline__ uint64_t l2_evict_first_policy()
+{
+    uint64_t policy;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+    return policy;
+}
+
+// bulk_copy_g2s with an L2 cache policy for the source lines.
+__device__ __forceinline__ void bulk_copy_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                                   uint64_t policy)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
 // Asks L2 to fetch `bytes` (a multiple of 16, 16-byte aligned address) of
 // global memory.  A hint: nothing lands in the CTA, nothing completes on a
 // barrier, and L2 stays coherent with every later write to those lines.
