@@ -45,17 +45,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return done != 0;
 }
 
-// Global memory -> shared memory, `bytes` (a multiple of 16, both addresses
-// 16-byte aligned), completion counted on `bar`.
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
 // An L2 cache policy for data read once: its lines are the first L2 gives
 // up when it needs room, so they do not push out lines still wanted (the
 // rows the next launch prefetched, blocks not yet written back).
@@ -66,7 +55,17 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy()
     return policy;
 }
 
-// bulk_copy_g2s with an L2 cache policy for the source lines.
+// The same for half of the lines (the others keep the normal policy).
+__device__ __forceinline__ uint64_t l2_evict_first_half_policy()
+{
+    uint64_t policy;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 0.5;" : "=l"(policy));
+    return policy;
+}
+
+// Global memory -> shared memory, `bytes` (a multiple of 16, both addresses
+// 16-byte aligned), completion counted on `bar`; the source lines get the L2
+// cache policy `policy`.
 __device__ __forceinline__ void bulk_copy_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
                                                    uint64_t policy)
 {

@@ -172,9 +172,10 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
     if (warp == compute_warps) {  // producer
         if (lane != 0) return;
         // Rows are read once: evict-first in L2 (single-codec launches back to
-        // back: 4096^2 ETC1s 12.3 against 13.2 us, BC1 11.2 against 12.4 us;
-        // the two-codec pass measured 0.9 us slower with it at 8192^2).
-        const uint64_t policy = l2_evict_first_policy();
+        // back: 4096^2 ETC1s 12.3 against 13.2 us, BC1 11.2 against 12.4 us).
+        // The two-codec pass marks half of them: with all it measured 0.9 us
+        // slower at 8192^2; with half, as fast there and 0.4 us faster at 4096^2.
+        const uint64_t policy = CODEC == kBoth ? l2_evict_first_half_policy() : l2_evict_first_policy();
         uint32_t issued = 0, slot = 0, phase = 0;
         for (uint32_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
             if (issued >= L.stages && !mbar_wait(&empty[slot], phase ^ 1u, &abort_flag, &g_pipeline_timeouts))
@@ -188,12 +189,8 @@ __global__ void __launch_bounds__(COMPUTE + 32, tma_min_ctas(BPT, COMPUTE))
             const uint8_t* row = src + (size_t)by * 4u * stride + 16u * (size_t)bx0;
             uint8_t* buf = smem + slot * L.stage_bytes;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                if constexpr (CODEC == kBoth)
-                    bulk_copy_g2s(buf + r * L.row_bytes, row + r * stride, bytes, &full[slot]);
-                else
-                    bulk_copy_g2s_hint(buf + r * L.row_bytes, row + r * stride, bytes, &full[slot], policy);
-            }
+            for (int r = 0; r < 4; ++r)
+                bulk_copy_g2s_hint(buf + r * L.row_bytes, row + r * stride, bytes, &full[slot], policy);
             ++issued;
             if (++slot == L.stages) {
                 slot = 0;
